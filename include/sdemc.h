@@ -1,0 +1,262 @@
+/*
+ * sdemc.h — C ABI of the GB300 (sm_103a) Monte Carlo path-integration library.
+ *
+ * Everything here is plain C: POD descriptors, raw pointers, sizes and a
+ * cudaStream_t passed as void*.  No torch types cross this boundary.  All
+ * array arguments named d_* are caller-owned DEVICE memory; h_* are host
+ * memory.  The library never allocates per call.  Every entry point returns an
+ * int status (SDEMC_OK == 0); sdemc_last_error() gives the message of the last
+ * failure on the calling thread.
+ *
+ * The reference (piers-hinds/sde_mc, pure Python on PyTorch) has no native
+ * code; each entry point below replaces a torch op chain of the reference and
+ * cites the Python it stands in for (path:line inside the sde_mc project).
+ */
+#ifndef SDEMC_H
+#define SDEMC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SDEMC_ABI_VERSION 1
+#define SDEMC_MAX_DIM 8
+#define SDEMC_CHOL_LEN 36       /* packed lower triangle of an 8x8 matrix */
+#define SDEMC_MARK_PARAMS 12
+#define SDEMC_CHUNK_PATHS 128   /* paths per reduction slot: 32 lanes x 4 rounds */
+
+/* ---- status codes ---------------------------------------------------- */
+enum {
+  SDEMC_OK = 0,
+  SDEMC_EINVAL = 1,        /* bad argument (shape, size, null pointer)          */
+  SDEMC_EUNSUPPORTED = 2,  /* model/payoff/dim combination not implemented      */
+  SDEMC_ENOMEM = 3,        /* caller buffer too small / admission over budget   */
+  SDEMC_ETIMEOUT = 4,      /* a bounded device loop gave up                     */
+  SDEMC_ECUDA = 5,         /* CUDA runtime error                                */
+  SDEMC_EOVERFLOW = 6      /* a path needed more steps/jumps than storage holds */
+};
+
+/* ---- descriptor enums ------------------------------------------------- */
+/* noise layout (Sde.diffusion_struct, sde_mc/sde.py:20-32)                  */
+enum {
+  SDEMC_NOISE_DIAG = 0,          /* dW = L z sqrt(dt)                          */
+  SDEMC_NOISE_INDEP_SHARED = 1,  /* jump solver 'indep': [L z, z'] with one
+                                    shared uncorrelated scalar z'
+                                    (sde_mc/solvers.py:197-201)               */
+  SDEMC_NOISE_INDEP_PAIR = 2     /* diffusion solver 'indep': two correlated
+                                    BMs L z1, L z2 (sde_mc/solvers.py:79-81)  */
+};
+/* time grid (which solver family)                                          */
+enum {
+  SDEMC_GRID_ADAPTED = 0,  /* JumpDiffusionSolver.solve, sde_mc/solvers.py:164-226 */
+  SDEMC_GRID_UNIFORM = 1   /* DiffusionSolver.solve,     sde_mc/solvers.py:68-88   */
+};
+/* jump mark law                                                            */
+enum {
+  SDEMC_MARK_NONE = 0,
+  SDEMC_MARK_LOGNORMAL = 1,  /* exp(N(alpha, gamma)) - 1, sde_mc/sde.py:325-326 */
+  SDEMC_MARK_INVCDF = 2      /* InverseCdf of a truncated Levy measure,
+                                sde_mc/levy.py:10-30, 85-87                    */
+};
+/* which components a jump event moves                                      */
+enum {
+  SDEMC_JUMP_COMMON = 0,     /* one scalar mark repeated over all dims
+                                (sde_mc/solvers.py:146-148)                   */
+  SDEMC_JUMP_ONE_ASSET = 1   /* superposition of independent per-asset
+                                compound Poisson processes: each event picks
+                                asset k with probability rate_k / sum(rate)   */
+};
+/* payoffs (sde_mc/options.py:179-321)                                      */
+enum {
+  SDEMC_PAYOFF_EUROCALL = 0,
+  SDEMC_PAYOFF_EUROPUT = 1,
+  SDEMC_PAYOFF_BINARY_AON = 2,
+  SDEMC_PAYOFF_BASKET_ARITH = 3,
+  SDEMC_PAYOFF_BASKET_GEO = 4,
+  SDEMC_PAYOFF_RAINBOW = 5,
+  SDEMC_PAYOFF_DIGITAL = 6,
+  SDEMC_PAYOFF_BESTOF = 7,
+  SDEMC_PAYOFF_ASIANCALL = 8,
+  SDEMC_PAYOFF_HESTON_RAINBOW = 9
+};
+
+/*
+ * One pricing instance: an affine-in-state SDE, its jump law, its time grid,
+ * the payoff and the RNG stream.  Component i of the state moves by
+ *
+ *   dx_i = (a_i + b_i x_i) dt + (s_i + q_i x_i) dW_i
+ *          [+ (s2_i + q2_i x_i) dW2_i]           (INDEP layouts)
+ *          + (g_i + k_i x_i^-) J                  (at a jump)
+ *
+ * which covers Gbm, LogGbm, DoubleGbm, Merton (sde_mc/sde.py:179-375) and the
+ * LevySde adapters (sde_mc/levy.py:65-192).  Scalars are float32 exactly as
+ * the reference evaluates them (the host lowering computes them with the
+ * reference's own float32 expressions).
+ */
+typedef struct sdemc_inst {
+  int32_t dim;          /* 1..SDEMC_MAX_DIM                                 */
+  int32_t noise;        /* SDEMC_NOISE_*                                    */
+  int32_t grid;         /* SDEMC_GRID_*                                     */
+  int32_t num_steps;    /* nominal steps; h = fl32(T / num_steps)           */
+  int32_t mark;         /* SDEMC_MARK_*                                     */
+  int32_t jump_target;  /* SDEMC_JUMP_*                                     */
+  int32_t exact_jumps;  /* 0: jump scaled by the pre-step state (reference
+                           default), 1: by the post-diffusion state         */
+  int32_t payoff;       /* SDEMC_PAYOFF_*                                   */
+  int32_t payoff_log;   /* Option.log: exp() the state before the payoff    */
+  int32_t flags;        /* SDEMC_INST_* bits                                */
+  uint32_t stream_id;   /* RNG substream (MLMC level, request id ...)       */
+  uint32_t reserved0;
+  uint64_t seed;        /* RNG key                                          */
+  uint64_t path_offset; /* global index of this instance's first path      */
+  int64_t num_paths;
+  float T;              /* time_interval, float32                           */
+  float h;              /* fl32(T / num_steps)                              */
+  float rate;           /* total jump intensity sum(jump_rate()), 0 = none  */
+  float inv_rate;       /* fl32(1 / rate)                                   */
+  float strike;
+  float payoff_scale;   /* Option.discount                                  */
+  float discount;       /* discounter(T) as float32                         */
+  float disc_rate;      /* ConstantShortRate.r (for per-step discounting)   */
+  float x0[SDEMC_MAX_DIM];
+  float drift_a[SDEMC_MAX_DIM], drift_b[SDEMC_MAX_DIM];
+  float diff_s[SDEMC_MAX_DIM], diff_q[SDEMC_MAX_DIM];
+  float diff2_s[SDEMC_MAX_DIM], diff2_q[SDEMC_MAX_DIM];
+  float jump_g[SDEMC_MAX_DIM], jump_k[SDEMC_MAX_DIM];
+  float jump_cdf[SDEMC_MAX_DIM];  /* ONE_ASSET: cumulative pick probabilities */
+  float chol[SDEMC_CHOL_LEN];     /* Cholesky factor of corr, packed rows     */
+  float mark_p[SDEMC_MARK_PARAMS];/* LOGNORMAL: alpha, gamma.
+                                     INVCDF: cm, cp, mu, alpha, eps, lda,
+                                     y1, y2, y3, uniform_shift              */
+} sdemc_inst;
+
+/* Launch tuning; all-zero means "choose for me". */
+typedef struct sdemc_cfg {
+  int32_t block_threads;   /* threads per CTA (multiple of 32), 0 = auto    */
+  int32_t ctas_per_sm;     /* persistent grid = SMs x this, 0 = auto        */
+  int32_t interleave;      /* path rounds a lane runs together: 1, 2 or 4   */
+  int32_t flags;           /* SDEMC_CFG_*                                   */
+  int64_t timeout_ns;      /* bound for device-side waits, 0 = default      */
+} sdemc_cfg;
+
+enum { SDEMC_CFG_EXACT_EULER = 1 }; /* use the reference's unfused op order */
+
+/* sdemc_inst.flags */
+enum {
+  /* Evaluate the payoff on the state after num_steps steps instead of the
+     terminal state: what mc_simple(payoff_time='terminal') reads from a jump
+     solver's storage (paths[:, num_steps], sde_mc/mc.py:84-86, 92).        */
+  SDEMC_INST_PAYOFF_AT_NOMINAL_STEP = 1
+};
+
+/* ---- library / device info ------------------------------------------ */
+int sdemc_abi_version(void);
+size_t sdemc_inst_size(void);
+/* offsetof() of every sdemc_inst field in declaration order (count in *n). */
+int sdemc_inst_offsets(size_t* h_offsets, int* n);
+int sdemc_last_error(char* h_buf, size_t len);
+int sdemc_device_sms(int* h_sms);
+/* FP32 FMA throughput probe (no reference counterpart): launches 8 CTAs of
+ * 256 threads per SM running 8 independent FMA chains for `iters` x 4 steps;
+ * *h_flops receives the flops of the launch (time it with events on the
+ * stream).  d_sink (sink_len floats) only keeps the chains live.           */
+int sdemc_fp32_probe(int iters, float* d_sink, int sink_len, double* h_flops,
+                     void* stream);
+
+/* ---- K1: fused pricing ------------------------------------------------
+ * Replaces mc_simple (sde_mc/mc.py:53-123) over JumpDiffusionSolver.solve
+ * (sde_mc/solvers.py:164-226) / DiffusionSolver.solve (:68-88), payoff
+ * (sde_mc/options.py:175-176) and mc_estimates (sde_mc/helpers.py:51-68).
+ * Every path lives in registers; per-chunk (sum, sum_sq, n) go to d_scratch;
+ * d_out receives (sum, sum_sq, n, mean, var, status) in FP64, status being a
+ * SDEMC_* code raised on the device (e.g. SDEMC_EOVERFLOW).  d_payoffs
+ * (nullable) receives each path's discounted payoff.  d_scratch must be
+ * zeroed before its first use; every call leaves its status word at zero.   */
+size_t sdemc_price_scratch_bytes(const sdemc_inst* h_inst);
+int sdemc_price(const sdemc_inst* h_inst, const sdemc_cfg* h_cfg,
+                void* d_scratch, size_t scratch_bytes, double* d_out,
+                float* d_payoffs, void* stream);
+/* The two halves of sdemc_price: the path kernel writing the chunk partials
+ * into d_scratch, and the FP64 reduction K10 of `nchunks` partials of `width`
+ * doubles (3 for prices, 5 for MLMC levels) into d_out (sums, mean, var,
+ * status).  nchunks = ceil(num_paths / SDEMC_CHUNK_PATHS).                 */
+int sdemc_price_chunks(const sdemc_inst* h_inst, const sdemc_cfg* h_cfg,
+                       void* d_scratch, size_t scratch_bytes, float* d_payoffs,
+                       void* stream);
+int sdemc_reduce_chunks(void* d_scratch, int64_t nchunks, int width,
+                        double* d_out, void* stream);
+
+/* ---- K3: replay of recorded draws --------------------------------------
+ * Runs the reference's jump-adapted loop (sde_mc/solvers.py:164-226, or its
+ * uniform-grid twin :68-88) on draws exported from the reference: d_jump_times
+ * (bs, max_jumps) cumulative jump times, d_dw (bs, S, dim[, 2]) the per-step
+ * noise exactly as the reference fed it to the scheme, d_marks (bs, S) the
+ * per-step mark, d_asset (bs, S, nullable) the picked asset for ONE_ASSET.
+ * Writes the AdaptedPathData layout (sde_mc/nets.py:192-207) at S+1 columns:
+ * d_paths/d_left/d_jumps (bs, S+1, dim), d_time (bs, S+1), and d_payoffs (bs).
+ * d_steps (bs) receives each path's own step count.                         */
+int sdemc_replay(const sdemc_inst* h_inst, int bs, int steps_cap,
+                 int max_jumps, const float* d_jump_times, const float* d_dw,
+                 const float* d_marks, const int32_t* d_asset, float* d_paths,
+                 float* d_left, float* d_time, float* d_jumps,
+                 float* d_payoffs, int32_t* d_steps, int32_t* d_status,
+                 void* stream);
+
+/* ---- K4: materialised paths -------------------------------------------
+ * JumpDiffusionSolver.solve / DiffusionSolver.solve with full storage
+ * (sde_mc/solvers.py:150-162, 205-222): paths/left/jumps (N, S+1, dim), time
+ * (N, S+1), normals (N, S, dim[, 2]), payoffs (N), per-path step counts.
+ * Optional export of the raw draws for the oracle: d_z (N, S, zdim) standard
+ * normals before scaling, d_jt (N, jcap) jump times, d_jm (N, jcap) marks.
+ * Every pointer may be NULL (d_jsel holds the ONE_ASSET picks).  S =
+ * steps_cap; paths needing more steps set *d_status = SDEMC_EOVERFLOW.
+ * Columns after a path's last step hold its frozen state (dt = 0).          */
+int sdemc_materialise(const sdemc_inst* h_inst, int steps_cap, float* d_paths,
+                      float* d_left, float* d_time, float* d_jumps,
+                      float* d_normals, float* d_payoffs, int32_t* d_steps,
+                      float* d_z, int zdim, float* d_jt, float* d_jm,
+                      int32_t* d_jsel, int jcap, int32_t* d_status,
+                      void* stream);
+
+/* ---- K2: MLMC level ----------------------------------------------------
+ * One level of mc_multilevel (sde_mc/mlmc.py:57-69) over the coupled
+ * JumpDiffusionSolver.multilevel_solve (sde_mc/solvers.py:228-307): fine and
+ * coarse paths run in the same thread from the same increments and marks.
+ * d_out receives (sum Y, sum Y^2, n, sum Pf, sum Pf^2, mean, var, status)
+ * with Y = disc*(payoff(fine) - payoff(coarse)) and Pf = disc*payoff(fine).
+ * The uniform grid couples DiffusionSolver.multilevel_solve (:90-119).      */
+size_t sdemc_mlmc_scratch_bytes(const sdemc_inst* h_inst);
+int sdemc_mlmc_level(const sdemc_inst* h_inst, int fine, int coarse,
+                     float h_fine, float h_coarse, const sdemc_cfg* h_cfg,
+                     void* d_scratch, size_t scratch_bytes, double* d_out,
+                     float* d_y, void* stream);
+
+/* Terminal fine/coarse states of num_paths coupled paths (d_xf, d_xc:
+ * (num_paths, dim)), i.e. multilevel_solve's last columns.                  */
+int sdemc_mlmc_terminals(const sdemc_inst* h_inst, int fine, int coarse,
+                         float h_fine, float h_coarse, float* d_xf, float* d_xc,
+                         int32_t* d_status, void* stream);
+
+/* MLMC replay on recorded draws: d_dw (bs, Sf, dim) per fine step, d_marks
+ * (bs, Sc) per coarse step.  Writes terminal fine/coarse states (bs, dim).  */
+int sdemc_mlmc_replay(const sdemc_inst* h_inst, int fine, int coarse,
+                      float h_fine, float h_coarse, int bs, int fine_cap,
+                      int coarse_cap, int max_jumps, const float* d_jump_times,
+                      const float* d_dw, const float* d_marks,
+                      const int32_t* d_asset, float* d_xf, float* d_xc,
+                      int32_t* d_status, void* stream);
+
+/* ---- RNG export (for the oracle and for users who want the raw draws) --
+ * Philox4x32-10 blocks for counter (c0 = first_block + i, c1 = path lo,
+ * c2 = path hi | tag << 16, c3 = stream_id), key = seed.                   */
+int sdemc_philox(uint64_t seed, uint32_t stream_id, uint32_t tag,
+                 uint64_t path, uint32_t first_block, int nblocks,
+                 uint32_t* d_out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SDEMC_H */

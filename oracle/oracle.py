@@ -1,0 +1,272 @@
+"""CPU oracle for the sde_mc path-integration hot path.
+
+TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the
+cpu_baseline leg of bench.py may import this module, and only as the checker
+(or the timed CPU baseline) — the product package never imports it.
+
+Contents (each restating the reference, piers-hinds/sde_mc):
+  * ctypes access to the C restatement ``sdemc_oracle.c`` of the solver loops
+    (sde_mc/solvers.py:68-88, 164-226, 228-307), payoffs and reductions;
+  * FP64 closed forms: Black-Scholes call and digital, asset-or-nothing,
+    geometric Asian and the 40-term Merton series (sde_mc/options.py:8-153);
+  * mc_estimates (sde_mc/helpers.py:51-68) and Giles' MLMC allocation
+    (sde_mc/mlmc.py:77-97);
+  * the control-variate MLP (sde_mc/nets.py:39-93 without batch norm), its
+    variance loss (sde_mc/varred.py:160-177, 202-214) with hand-derived
+    gradients, and one Adam step, in numpy FP64.
+
+Parity is pinned against the reference itself through the fixtures in
+tests/golden/ (recorded by tests/golden/make_golden.py from the reference).
+"""
+import ctypes
+import math
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "libsdemc_oracle.so")
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            from . import build as _b  # noqa
+            _b.build()
+        lib = ctypes.CDLL(LIB)
+        P, I, F = ctypes.c_void_p, ctypes.c_int, ctypes.c_float
+        I64 = ctypes.c_int64
+        sig = {
+            "oracle_philox": (None, [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64,
+                                     ctypes.c_uint32, I, P]),
+            "oracle_native_normals": (None, [P, I64, I, P]),
+            "oracle_native_jumps": (None, [P, I64, I, P, P, P]),
+            "oracle_replay": (I, [P, I, I, I, P, P, P, P, P, P, P, P, P, P]),
+            "oracle_from_export": (I, [P, I64, I, P, I, P, P, P, I, I, P, P, P, P, P, P, P]),
+            "oracle_mlmc_replay": (I, [P, I, F, F, I, I, I, I, P, P, P, P, P, P]),
+            "oracle_price": (I, [P, I, P, P]),
+            "oracle_mlmc_level": (I, [P, I, F, F, I, P, P]),
+            "oracle_chunk_reduce": (None, [P, P, I64, P]),
+            "oracle_payoff": (F, [P, P]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def _p(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+def _c(a, dt=np.float32):
+    return None if a is None else np.ascontiguousarray(a, dtype=dt)
+
+
+# --------------------------------------------------------------- RNG -------
+def philox(seed, stream, tag, path, first, n):
+    out = np.zeros((n, 4), np.uint32)
+    load().oracle_philox(seed, stream, tag, path, first, n, _p(out))
+    return out
+
+
+def native_normals(inst, path, nsteps, zdim):
+    out = np.zeros((nsteps, zdim), np.float32)
+    load().oracle_native_normals(ctypes.byref(inst), path, nsteps, _p(out))
+    return out
+
+
+def native_jumps(inst, path, n):
+    jt = np.zeros(n, np.float32)
+    jm = np.zeros(n, np.float32)
+    js = np.zeros(n, np.int32)
+    load().oracle_native_jumps(ctypes.byref(inst), path, n, _p(jt), _p(jm), _p(js))
+    return jt, jm, js
+
+
+# ----------------------------------------------------------- solvers -------
+def replay(inst, dw, jump_times=None, marks=None, asset=None):
+    dw = _c(dw)
+    bs, S = dw.shape[0], dw.shape[1]
+    d = inst.dim
+    jump_times, marks, asset = _c(jump_times), _c(marks), _c(asset, np.int32)
+    out = dict(paths=np.zeros((bs, S + 1, d), np.float32), left=np.zeros((bs, S + 1, d), np.float32),
+               time=np.zeros((bs, S + 1), np.float32), jumps=np.zeros((bs, S + 1, d), np.float32),
+               payoffs=np.zeros(bs, np.float32), steps=np.zeros(bs, np.int32))
+    mj = jump_times.shape[1] if jump_times is not None else 0
+    rc = load().oracle_replay(ctypes.byref(inst), bs, S, mj, _p(jump_times), _p(dw), _p(marks), _p(asset),
+                              _p(out["paths"]), _p(out["left"]), _p(out["time"]), _p(out["jumps"]),
+                              _p(out["payoffs"]), _p(out["steps"]))
+    out["rc"] = rc
+    return out
+
+
+def from_export(inst, z, S, jt=None, jm=None, jsel=None, exact=False):
+    """Re-run paths from raw draws a GPU materialise call exported."""
+    z = _c(z)
+    n, zd = z.shape[0], z.shape[2]
+    d = inst.dim
+    nw = 1 if inst.noise == 0 else 2
+    jt, jm, jsel = _c(jt), _c(jm), _c(jsel, np.int32)
+    jcap = jt.shape[1] if jt is not None else 0
+    out = dict(paths=np.zeros((n, S + 1, d), np.float32), left=np.zeros((n, S + 1, d), np.float32),
+               time=np.zeros((n, S + 1), np.float32), jumps=np.zeros((n, S + 1, d), np.float32),
+               normals=np.zeros((n, S, d) if nw == 1 else (n, S, d, 2), np.float32),
+               payoffs=np.zeros(n, np.float32), steps=np.zeros(n, np.int32))
+    rc = load().oracle_from_export(ctypes.byref(inst), n, S, _p(z), zd, _p(jt), _p(jm), _p(jsel), jcap,
+                                   1 if exact else 0, _p(out["paths"]), _p(out["left"]), _p(out["time"]),
+                                   _p(out["jumps"]), _p(out["normals"]), _p(out["payoffs"]), _p(out["steps"]))
+    out["rc"] = rc
+    return out
+
+
+def mlmc_replay(inst, factor, hf, hc, dw, coarse_cap, jump_times=None, marks=None, asset=None):
+    dw = _c(dw)
+    bs, Sf = dw.shape[0], dw.shape[1]
+    d = inst.dim
+    jump_times, marks, asset = _c(jump_times), _c(marks), _c(asset, np.int32)
+    xf = np.zeros((bs, d), np.float32)
+    xc = np.zeros((bs, d), np.float32)
+    mj = jump_times.shape[1] if jump_times is not None else 0
+    rc = load().oracle_mlmc_replay(ctypes.byref(inst), factor, hf, hc, bs, Sf, coarse_cap, mj, _p(jump_times),
+                                   _p(dw), _p(marks), _p(asset), _p(xf), _p(xc))
+    return dict(xf=xf, xc=xc, rc=rc)
+
+
+def price(inst, nthreads=None, payoffs=False):
+    """Native-draw pricing on host threads: (sum, sum_sq, n, mean, var)."""
+    nthreads = nthreads or os.cpu_count() or 1
+    out = np.zeros(7, np.float64)
+    pay = np.zeros(inst.num_paths, np.float32) if payoffs else None
+    rc = load().oracle_price(ctypes.byref(inst), nthreads, _p(pay), _p(out))
+    return out, pay, rc
+
+
+def mlmc_level(inst, factor, hf, hc, nthreads=None):
+    nthreads = nthreads or os.cpu_count() or 1
+    out = np.zeros(7, np.float64)
+    rc = load().oracle_mlmc_level(ctypes.byref(inst), factor, hf, hc, nthreads, None, _p(out))
+    return out, rc
+
+
+def chunk_reduce(vals, vals2=None):
+    """The GPU kernels' reduction order restated (bit-exact given the values)."""
+    vals = _c(vals)
+    vals2 = _c(vals2)
+    out = np.zeros(7 if vals2 is not None else 5, np.float64)
+    load().oracle_chunk_reduce(_p(vals), _p(vals2), vals.shape[0], _p(out))
+    return out
+
+
+# ------------------------------------------------------ closed forms -------
+def norm_cdf(x):
+    return 0.5 * math.erfc(-x / math.sqrt(2.0))
+
+
+def bs_call(spot, strike, expiry, r, sigma):
+    sd = sigma * math.sqrt(expiry)
+    d1 = (math.log(spot / strike) + (r + 0.5 * sigma * sigma) * expiry) / sd
+    return spot * norm_cdf(d1) - strike * math.exp(-r * expiry) * norm_cdf(d1 - sd)
+
+
+def bs_binary_aon(spot, strike, expiry, r, sigma):
+    """The reference integrates exp(-z^2/2)/sqrt(2 pi) up to d1 (quad): Phi(d1)."""
+    d1 = (math.log(spot / strike) + (r + 0.5 * sigma * sigma) * expiry) / (math.sqrt(expiry) * sigma)
+    return norm_cdf(d1)
+
+
+def merton_call(spot, strike, expiry, r, sigma, alpha, gamma, rate, terms=40):
+    beta = math.exp(alpha + 0.5 * gamma * gamma) - 1
+    lam = (1 + beta) * rate * expiry
+    total = 0.0
+    for k in range(terms):
+        r_k = r - rate * beta + k * math.log1p(beta) / expiry
+        s_k = math.sqrt(sigma * sigma + k * gamma * gamma / expiry)
+        total += math.exp(-lam) * lam ** k / math.factorial(k) * bs_call(spot, strike, expiry, r_k, s_k)
+    return total
+
+
+def bs_digital_call(spot, strike, expiry, r, sigma):
+    sd = sigma * math.sqrt(expiry)
+    d2 = (math.log(spot / strike) + (r - 0.5 * sigma * sigma) * expiry) / sd
+    return norm_cdf(d2) * math.exp(-r * expiry)
+
+
+def bs_asian_call(spot, strike, expiry, r, sigma):
+    sg = sigma / math.sqrt(3)
+    b = 0.5 * (r - 0.5 * sg * sg)
+    sd = sg * math.sqrt(expiry)
+    d1 = (math.log(spot / strike) + (b + 0.5 * sg * sg) * expiry) / sd
+    return spot * math.exp((b - r) * expiry) * norm_cdf(d1) - strike * math.exp(-r * expiry) * norm_cdf(d1 - sd)
+
+
+# -------------------------------------------------------- estimators -------
+def mc_estimates(s, s2, n):
+    return s / n, (s2 - s * s / n) / (n - 1)
+
+
+def optimal_trials(level_vars, levels, T, eps):
+    v = np.asarray(level_vars, np.float64)
+    h = T / np.asarray(levels, np.float64)
+    return np.ceil((1.96 ** 2 / eps ** 2) * np.sqrt(v * h) * np.sqrt(v / h).sum()).astype(np.int64)
+
+
+# ----------------------------------------------------------- CV MLP --------
+def mlp_forward(params, x):
+    """params: [W0, b0, W1, b1, ..., WL, bL] with W (out, in) as torch Linear.
+    Returns output and the list of pre-activations / activations."""
+    acts = [x]
+    pre = []
+    h = x
+    nl = len(params) // 2
+    for i in range(nl):
+        W, b = params[2 * i], params[2 * i + 1]
+        z = h @ W.T + b
+        pre.append(z)
+        h = np.maximum(z, 0.0) if i < nl - 1 else z
+        acts.append(h)
+    return h, pre, acts
+
+
+def cv_loss_and_grads(params, f_in, normals, time, payoffs, r):
+    """Gamma = payoff + sum_k e^{-r t_k} f(t_k, X_k) . dW_k; loss = Var(Gamma)
+    (unbiased); gradients by hand-written backpropagation."""
+    n, S, d = normals.shape
+    out, pre, acts = mlp_forward(params, f_in)
+    disc = np.exp(-time * r)[..., None] if time.ndim == 2 else np.exp(-time * r)
+    fo = out.reshape(n, S, d)
+    gamma = payoffs + (normals * fo * disc).sum(-1).sum(-1)
+    gm = gamma.mean()
+    loss = ((gamma - gm) ** 2).sum() / (n - 1)
+    dgamma = 2.0 * (gamma - gm) / (n - 1)
+    dout = (dgamma[:, None, None] * normals * disc).reshape(n * S, d)
+    grads = [None] * len(params)
+    g = dout
+    nl = len(params) // 2
+    for i in reversed(range(nl)):
+        W = params[2 * i]
+        grads[2 * i] = g.T @ acts[i]
+        grads[2 * i + 1] = g.sum(0)
+        if i > 0:
+            g = (g @ W) * (pre[i - 1] > 0)
+    return loss, gamma, grads
+
+
+def adam_step(params, grads, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8, state=None, step=1):
+    """One torch.optim.Adam step (no weight decay, no amsgrad)."""
+    if state is None:
+        state = [(np.zeros_like(p), np.zeros_like(p)) for p in params]
+    new, st = [], []
+    for p, g, (m, v) in zip(params, grads, state):
+        m = b1 * m + (1 - b1) * g
+        v = b2 * v + (1 - b2) * g * g
+        mh = m / (1 - b1 ** step)
+        vh = v / (1 - b2 ** step)
+        new.append(p - lr * mh / (np.sqrt(vh) + eps))
+        st.append((m, v))
+    return new, st

@@ -1,0 +1,669 @@
+/*
+ * sdemc_oracle.c — CPU oracle for the sde_mc path-integration hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the
+ * cpu_baseline leg of bench.py may load this library, and only as the
+ * checker or as the timed CPU baseline — never as part of the product path.
+ *
+ * A plain-C restatement of the reference's algorithm (piers-hinds/sde_mc):
+ *   - the jump-adapted Euler loop of JumpDiffusionSolver.solve
+ *     (sde_mc/solvers.py:164-226): h = min(h, max(T - t, 0)),
+ *     dt = min(h, next_jump - t), x += drift*dt + diffusion*dW, t += dt, and a
+ *     jump when torch.isclose(next_jump, t, atol=1e-12) (rtol 1e-5), applied
+ *     with the pre-step state unless exact_jumps (:212-217);
+ *   - the uniform grid of DiffusionSolver.solve (sde_mc/solvers.py:68-88);
+ *   - the coupled fine/coarse loop of multilevel_solve (:228-307);
+ *   - EulerScheme.step (sde_mc/schemes.py:6-13), the Merton/Gbm/Levy affine
+ *     coefficients (sde_mc/sde.py:203-219, 368-375; sde_mc/levy.py:74-83);
+ *   - Option payoffs (sde_mc/options.py:167-321) and mc_estimates
+ *     (sde_mc/helpers.py:51-68).
+ * Draw sources: (1) arrays recorded from the reference (replay), (2) the raw
+ * draws a GPU run exported (so the GPU is checked step by step), (3) its own
+ * Philox4x32-10 streams with libm transforms (the CPU baseline).  Float
+ * arithmetic is written op by op (compile with -ffp-contract=off) so modes
+ * (1)/(2) reproduce the GPU's rounding exactly.
+ */
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include "../include/sdemc.h"
+
+#define MAXD SDEMC_MAX_DIM
+
+/* ------------------------------------------------------------- Philox --- */
+static void philox(uint32_t c[4], uint32_t k0, uint32_t k1) {
+  for (int r = 0; r < 10; ++r) {
+    if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+    uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
+    uint64_t p1 = (uint64_t)0xCD9E8D57u * c[2];
+    uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0;
+    uint32_t n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1;
+    c[0] = n0; c[1] = (uint32_t)p1; c[2] = n2; c[3] = (uint32_t)p0;
+  }
+}
+
+typedef struct { uint32_t k0, k1, c1, c2base, c3; } skey_t;
+
+static void skey_init(skey_t* k, uint64_t seed, uint32_t stream, uint64_t gpath) {
+  k->k0 = (uint32_t)seed; k->k1 = (uint32_t)(seed >> 32);
+  k->c1 = (uint32_t)gpath; k->c2base = (uint32_t)(gpath >> 32) & 0xFFFFu; k->c3 = stream;
+}
+
+static void skey_block(const skey_t* k, uint32_t tag, uint32_t b, uint32_t out[4]) {
+  out[0] = b; out[1] = k->c1; out[2] = k->c2base | (tag << 16); out[3] = k->c3;
+  philox(out, k->k0, k->k1);
+}
+
+static float u01(uint32_t w) {
+  union { uint32_t u; float f; } v;
+  v.u = 0x3F800000u | (w >> 9);
+  return v.f - 0.99999994f;
+}
+
+static const float kTwoPi = 6.283185307179586f, kPi = 3.141592653589793f;
+
+static float bm_radius(uint32_t w) { return sqrtf(-2.0f * logf(u01(w))); }
+static float bm_angle(uint32_t w) { return fmaf(kTwoPi, u01(w), -kPi); }
+
+/* ------------------------------------------------------------- layout --- */
+static int zdim_of(int D, int noise) {
+  return noise == SDEMC_NOISE_DIAG ? D : noise == SDEMC_NOISE_INDEP_SHARED ? D + 1 : 2 * D;
+}
+static int nw_of(int noise) { return noise == SDEMC_NOISE_DIAG ? 1 : 2; }
+
+static float chol_at(const sdemc_inst* I, int i, int j) { return I->chol[i * (i + 1) / 2 + j]; }
+
+static void correlate(const sdemc_inst* I, int D, const float* z, float sq, float* dW) {
+  float zs[MAXD];
+  for (int j = 0; j < D; ++j) zs[j] = z[j] * sq;
+  if (D == 1) { dW[0] = zs[0]; return; }
+  for (int i = 0; i < D; ++i) {
+    float acc = chol_at(I, i, 0) * zs[0];
+    for (int j = 1; j <= i; ++j) acc = fmaf(chol_at(I, i, j), zs[j], acc);
+    dW[i] = acc;
+  }
+}
+
+/* ------------------------------------------------------------- draws ---- */
+enum { DRAW_NATIVE = 0, DRAW_REPLAY = 1, DRAW_EXPORT = 2 };
+
+typedef struct {
+  int mode;
+  /* replay */
+  const float* dw; const float* marks; const int32_t* asset; const float* jt; int S; int MJ;
+  /* export */
+  const float* z; int zdim; const float* xjt; const float* xjm; const int32_t* xjsel; int jcap;
+  /* native */
+  skey_t key; float buf[4]; uint32_t jblock; float jmark; int jsel;
+  /* state */
+  int jidx; int overflow; float sq_h, h_nom;
+} draws_t;
+
+static float inverse_cdf(const sdemc_inst* I, float y) {
+  const float cm = I->mark_p[0], cp = I->mark_p[1], mu = I->mark_p[2], al = I->mark_p[3];
+  const float lda = I->mark_p[5], y1 = I->mark_p[6], y2 = I->mark_p[7], y3 = I->mark_p[8];
+  const float epa = I->mark_p[10], nia = I->mark_p[11];
+  if (y <= y1) return logf((mu * lda * y) / cm) / mu - 1.0f;
+  if (y < y2) return -powf(al * ((lda * y / cm) - (1.0f / mu)) + 1.0f, nia);
+  if (y < y3) return powf((-al / cp) * (lda * y - cm / mu - cm * ((epa - 1.0f) / al)) + epa, nia);
+  return 1.0f - (1.0f / mu) * logf(mu * lda * (1.0f - y) / cp);
+}
+
+static float native_load_jump(const sdemc_inst* I, int D, draws_t* d, uint32_t j) {
+  uint32_t w[4];
+  skey_block(&d->key, 1u, j, w);
+  float gap = -logf(u01(w[0])) * I->inv_rate;
+  if (I->mark == SDEMC_MARK_LOGNORMAL) {
+    float zn = bm_radius(w[1]) * cosf(bm_angle(w[2]));
+    d->jmark = expf(I->mark_p[1] * zn + I->mark_p[0]) - 1.0f;
+  } else if (I->mark == SDEMC_MARK_INVCDF) {
+    d->jmark = inverse_cdf(I, u01(w[1]) + I->mark_p[9]);
+  } else {
+    d->jmark = 0.f;
+  }
+  d->jsel = 0;
+  if (I->jump_target == SDEMC_JUMP_ONE_ASSET) {
+    float us = u01(w[3]);
+    for (int i = 0; i < D - 1; ++i) d->jsel += (us >= I->jump_cdf[i]) ? 1 : 0;
+  }
+  return gap;
+}
+
+static void native_fill4(const draws_t* d, uint32_t b, float* o) {
+  uint32_t w[4];
+  skey_block(&d->key, 0u, b, w);
+  float r0 = bm_radius(w[0]), a0 = bm_angle(w[1]), r1 = bm_radius(w[2]), a1 = bm_angle(w[3]);
+  o[0] = r0 * cosf(a0); o[1] = r0 * sinf(a0); o[2] = r1 * cosf(a1); o[3] = r1 * sinf(a1);
+}
+
+static void native_normals(draws_t* d, int ZD, int k, float* z) {
+  if (ZD == 1 || ZD == 2) {
+    int pos = (k * ZD) & 3;
+    if (pos == 0) native_fill4(d, (uint32_t)((k * ZD) >> 2), d->buf);
+    for (int i = 0; i < ZD; ++i) z[i] = d->buf[pos + i];
+  } else {
+    int nb = (ZD + 3) / 4;
+    for (int b = 0; b < nb; ++b) {
+      float o[4];
+      native_fill4(d, (uint32_t)(k * nb + b), o);
+      for (int q = 0; q < 4; ++q) if (4 * b + q < ZD) z[4 * b + q] = o[q];
+    }
+  }
+}
+
+static void draws_increments(const sdemc_inst* I, int D, draws_t* d, int k, float dt,
+                             float* dW, float* dW2) {
+  const int noise = I->noise, ZD = zdim_of(D, noise), NW = nw_of(noise);
+  for (int i = 0; i < D; ++i) dW2[i] = 0.f;
+  if (d->mode == DRAW_REPLAY) {
+    if (k >= d->S) { for (int i = 0; i < D; ++i) dW[i] = 0.f; d->overflow = 1; return; }
+    const float* r = d->dw + (size_t)k * D * NW;
+    for (int i = 0; i < D; ++i) {
+      if (NW == 1) dW[i] = r[i];
+      else { dW[i] = r[2 * i]; dW2[i] = r[2 * i + 1]; }
+    }
+    return;
+  }
+  float z[2 * MAXD];
+  if (d->mode == DRAW_EXPORT) {
+    if (k >= d->S) { for (int j = 0; j < ZD; ++j) z[j] = 0.f; d->overflow = 1; }
+    else memcpy(z, d->z + (size_t)k * d->zdim, sizeof(float) * ZD);
+  } else {
+    native_normals(d, ZD, k, z);
+  }
+  const float sq = (dt == d->h_nom) ? d->sq_h : sqrtf(dt);
+  correlate(I, D, z, sq, dW);
+  if (noise == SDEMC_NOISE_INDEP_SHARED) {
+    float s = z[D] * sq;
+    for (int i = 0; i < D; ++i) dW2[i] = s;
+  } else if (noise == SDEMC_NOISE_INDEP_PAIR) {
+    correlate(I, D, z + D, sq, dW2);
+  }
+}
+
+static const float kInf = INFINITY;
+
+static float draws_jump_first(const sdemc_inst* I, int D, draws_t* d) {
+  d->jidx = 0;
+  if (I->rate <= 0.f) return kInf;
+  if (d->mode == DRAW_REPLAY) return d->MJ > 0 ? d->jt[0] : kInf;
+  if (d->mode == DRAW_EXPORT) return d->jcap > 0 ? d->xjt[0] : kInf;
+  d->jblock = 0;
+  return native_load_jump(I, D, d, 0);
+}
+
+static void draws_jump_mark(const draws_t* d, int k, float* J, int* sel) {
+  if (d->mode == DRAW_REPLAY) {
+    *J = k < d->S ? d->marks[k] : 0.f;
+    *sel = (d->asset && k < d->S) ? d->asset[k] : 0;
+  } else if (d->mode == DRAW_EXPORT) {
+    *J = d->jidx < d->jcap ? d->xjm[d->jidx] : 0.f;
+    *sel = (d->xjsel && d->jidx < d->jcap) ? d->xjsel[d->jidx] : 0;
+  } else {
+    *J = d->jmark; *sel = d->jsel;
+  }
+}
+
+static float draws_jump_next(const sdemc_inst* I, int D, draws_t* d, float nj) {
+  d->jidx++;
+  if (d->mode == DRAW_REPLAY) {
+    if (d->jidx >= d->MJ) { d->overflow = 1; return kInf; }
+    return d->jt[d->jidx];
+  }
+  if (d->mode == DRAW_EXPORT) {
+    if (d->jidx >= d->jcap) { d->overflow = 1; return kInf; }
+    return d->xjt[d->jidx];
+  }
+  d->jblock++;
+  return nj + native_load_jump(I, D, d, d->jblock);
+}
+
+/* ------------------------------------------------------------- scheme --- */
+static void euler(const sdemc_inst* I, int D, int exact, float* x, float dt, const float* dW,
+                  const float* dW2) {
+  for (int i = 0; i < D; ++i) {
+    float xi = x[i];
+    if (exact) {
+      float dr = I->drift_a[i] + I->drift_b[i] * xi;
+      float sg = I->diff_s[i] + I->diff_q[i] * xi;
+      float base = xi + dr * dt;
+      if (I->noise == SDEMC_NOISE_DIAG) x[i] = base + sg * dW[i];
+      else {
+        float sg2 = I->diff2_s[i] + I->diff2_q[i] * xi;
+        x[i] = base + (sg * dW[i] + sg2 * dW2[i]);
+      }
+    } else {
+      float dr = fmaf(I->drift_b[i], xi, I->drift_a[i]);
+      float sg = fmaf(I->diff_q[i], xi, I->diff_s[i]);
+      float xn = fmaf(dr, dt, xi);
+      xn = fmaf(sg, dW[i], xn);
+      if (I->noise != SDEMC_NOISE_DIAG) {
+        float sg2 = fmaf(I->diff2_q[i], xi, I->diff2_s[i]);
+        xn = fmaf(sg2, dW2[i], xn);
+      }
+      x[i] = xn;
+    }
+  }
+}
+
+static void apply_jump(const sdemc_inst* I, int D, int exact, float* x, const float* base, float J,
+                       int sel) {
+  int one = I->jump_target == SDEMC_JUMP_ONE_ASSET;
+  for (int i = 0; i < D; ++i) {
+    if (one && i != sel) continue;
+    if (exact) x[i] = x[i] + (I->jump_g[i] + I->jump_k[i] * base[i]) * J;
+    else x[i] = fmaf(fmaf(I->jump_k[i], base[i], I->jump_g[i]), J, x[i]);
+  }
+}
+
+static int jump_due(float nj, float t) {
+  float err = fabsf(nj - t);
+  float tol = 1e-12f + fabsf(1e-5f * t);
+  return (nj == t) || (err <= tol);
+}
+
+float oracle_payoff(const sdemc_inst* I, const float* xin) {
+  const int D = I->dim;
+  float s[MAXD];
+  for (int i = 0; i < D; ++i) {
+    float sp = I->payoff_log ? expf(xin[i]) : xin[i];
+    s[i] = I->payoff_scale * sp;
+  }
+  const float K = I->strike;
+  float m;
+  switch (I->payoff) {
+    case SDEMC_PAYOFF_EUROCALL: return s[0] > K ? s[0] - K : 0.f;
+    case SDEMC_PAYOFF_EUROPUT: return s[0] < K ? K - s[0] : 0.f;
+    case SDEMC_PAYOFF_BINARY_AON: return s[0] >= K ? s[0] : 0.f;
+    case SDEMC_PAYOFF_DIGITAL: return s[0] > K ? 1.f : 0.f;
+    case SDEMC_PAYOFF_BASKET_ARITH:
+      m = s[0];
+      for (int i = 1; i < D; ++i) m = m + s[i];
+      m = m / (float)D;
+      return m > K ? m - K : 0.f;
+    case SDEMC_PAYOFF_BASKET_GEO:
+      m = logf(s[0]);
+      for (int i = 1; i < D; ++i) m = m + logf(s[i]);
+      m = expf(m / (float)D);
+      return m > K ? m - K : 0.f;
+    case SDEMC_PAYOFF_RAINBOW:
+      m = s[0];
+      for (int i = 1; i < D; ++i) m = fmaxf(m, s[i]);
+      return m > K ? m - K : 0.f;
+    case SDEMC_PAYOFF_BESTOF:
+      m = s[0];
+      for (int i = 1; i < D; ++i) m = fmaxf(m, s[i]);
+      return fmaxf(m, K);
+    case SDEMC_PAYOFF_ASIANCALL: {
+      if (D < 2) return 0.f;
+      float a = s[1] / I->T;
+      float sp = I->payoff_log ? expf(a) : a;
+      return sp > K ? sp - K : 0.f;
+    }
+    case SDEMC_PAYOFF_HESTON_RAINBOW:
+      m = s[0];
+      for (int i = 2; i < D; i += 2) m = fmaxf(m, s[i]);
+      return m > K ? m - K : 0.f;
+    default: return 0.f;
+  }
+}
+
+/* One path of the reference loop.  Storage pointers may be NULL; when given
+ * they follow the AdaptedPathData layout with S = cap columns (+1). Returns
+ * the path's active step count (or -1 on overflow). A path runs alone here,
+ * so "frozen" steps of the batch-global loop are simply not taken; storage
+ * columns after the last step hold the frozen values. */
+static int run_path(const sdemc_inst* I, draws_t* d, int exact, int cap, float* paths, float* left,
+                    float* time, float* jumps, float* normals, float* x) {
+  const int D = I->dim, NW = nw_of(I->noise);
+  int jump_one = I->jump_target == SDEMC_JUMP_ONE_ASSET;
+  for (int i = 0; i < D; ++i) x[i] = I->x0[i];
+  if (paths) for (int i = 0; i < D; ++i) paths[i] = x[i];
+  if (left) for (int i = 0; i < D; ++i) left[i] = x[i];
+  if (jumps) for (int i = 0; i < D; ++i) jumps[i] = 0.f;
+  if (time) time[0] = 0.f;
+  float t = 0.f, dW[MAXD], dW2[MAXD], old[MAXD], xl[MAXD];
+  int k = 0;
+  if (I->grid == SDEMC_GRID_UNIFORM) {
+    for (; k < I->num_steps; ++k) {
+      draws_increments(I, D, d, k, I->h, dW, dW2);
+      euler(I, D, exact, x, I->h, dW, dW2);
+      t = t + I->h;
+      if (k < cap) {
+        size_t c = (size_t)(k + 1) * D;
+        if (paths) for (int i = 0; i < D; ++i) paths[c + i] = x[i];
+        if (left) for (int i = 0; i < D; ++i) left[c + i] = x[i];
+        if (jumps) for (int i = 0; i < D; ++i) jumps[c + i] = 0.f;
+        if (time) time[k + 1] = t;
+        if (normals) for (int i = 0; i < D; ++i) {
+          if (NW == 1) normals[(size_t)k * D + i] = dW[i];
+          else { normals[(size_t)k * D * 2 + 2 * i] = dW[i]; normals[(size_t)k * D * 2 + 2 * i + 1] = dW2[i]; }
+        }
+      }
+    }
+  } else {
+    const float T = I->T;
+    float h = I->h;
+    float nj = draws_jump_first(I, D, d);
+    int maxit = cap;
+    while (t < T) {
+      if (k >= maxit) return -1;
+      h = fminf(h, fmaxf(T - t, 0.f));
+      float dt = fminf(h, nj - t);
+      draws_increments(I, D, d, k, dt, dW, dW2);
+      memcpy(old, x, sizeof(float) * D);
+      euler(I, D, exact, x, dt, dW, dW2);
+      t = t + dt;
+      memcpy(xl, x, sizeof(float) * D);
+      float J = 0.f;
+      int sel = 0;
+      if (jump_due(nj, t)) {
+        draws_jump_mark(d, k, &J, &sel);
+        apply_jump(I, D, exact, x, I->exact_jumps ? x : old, J, sel);
+        nj = draws_jump_next(I, D, d, nj);
+      }
+      size_t c = (size_t)(k + 1) * D;
+      if (paths) for (int i = 0; i < D; ++i) paths[c + i] = x[i];
+      if (left) for (int i = 0; i < D; ++i) left[c + i] = xl[i];
+      if (jumps) for (int i = 0; i < D; ++i) jumps[c + i] = (jump_one && i != sel) ? 0.f : J;
+      if (time) time[k + 1] = t;
+      if (normals) for (int i = 0; i < D; ++i) {
+        if (NW == 1) normals[(size_t)k * D + i] = dW[i];
+        else { normals[(size_t)k * D * 2 + 2 * i] = dW[i]; normals[(size_t)k * D * 2 + 2 * i + 1] = dW2[i]; }
+      }
+      ++k;
+    }
+  }
+  for (int kk = k; kk < cap; ++kk) {
+    size_t c = (size_t)(kk + 1) * D;
+    if (paths) for (int i = 0; i < D; ++i) paths[c + i] = x[i];
+    if (left) for (int i = 0; i < D; ++i) left[c + i] = x[i];
+    if (jumps) for (int i = 0; i < D; ++i) jumps[c + i] = 0.f;
+    if (time) time[kk + 1] = t;
+    if (normals) for (int i = 0; i < D * NW; ++i) normals[(size_t)kk * D * NW + i] = 0.f;
+  }
+  return d->overflow ? -1 : k;
+}
+
+static void draws_native_init(const sdemc_inst* I, draws_t* d, int64_t p) {
+  memset(d, 0, sizeof(*d));
+  d->mode = DRAW_NATIVE;
+  skey_init(&d->key, I->seed, I->stream_id, I->path_offset + (uint64_t)p);
+  d->h_nom = I->h;
+  d->sq_h = sqrtf(I->h);
+}
+
+/* ------------------------------------------------------------- exports -- */
+
+void oracle_philox(uint64_t seed, uint32_t stream, uint32_t tag, uint64_t path, uint32_t first,
+                   int n, uint32_t* out) {
+  skey_t k;
+  skey_init(&k, seed, stream, path);
+  for (int i = 0; i < n; ++i) skey_block(&k, tag, first + (uint32_t)i, out + 4 * i);
+}
+
+/* Native standard normals of steps [0, nsteps) of one path: (nsteps, zdim). */
+void oracle_native_normals(const sdemc_inst* I, int64_t p, int nsteps, float* out) {
+  draws_t d;
+  draws_native_init(I, &d, p);
+  const int ZD = zdim_of(I->dim, I->noise);
+  for (int k = 0; k < nsteps; ++k) native_normals(&d, ZD, k, out + (size_t)k * ZD);
+}
+
+/* Native jump stream of one path: first n jump times, marks and picks. */
+void oracle_native_jumps(const sdemc_inst* I, int64_t p, int n, float* jt, float* jm, int32_t* js) {
+  draws_t d;
+  draws_native_init(I, &d, p);
+  float nj = draws_jump_first(I, I->dim, &d);
+  for (int j = 0; j < n; ++j) {
+    jt[j] = nj; jm[j] = d.jmark; js[j] = d.jsel;
+    if (I->rate > 0.f) nj = draws_jump_next(I, I->dim, &d, nj);
+  }
+}
+
+/* Replay recorded reference draws for bs paths (layouts as sdemc_replay). */
+int oracle_replay(const sdemc_inst* I, int bs, int S, int MJ, const float* jt, const float* dw,
+                  const float* marks, const int32_t* asset, float* paths, float* left, float* time,
+                  float* jumps, float* payoffs, int32_t* steps) {
+  const int D = I->dim, NW = nw_of(I->noise);
+  int bad = 0;
+  for (int p = 0; p < bs; ++p) {
+    draws_t d;
+    memset(&d, 0, sizeof(d));
+    d.mode = DRAW_REPLAY;
+    d.dw = dw + (size_t)p * S * D * NW;
+    d.marks = marks ? marks + (size_t)p * S : NULL;
+    d.asset = asset ? asset + (size_t)p * S : NULL;
+    d.jt = jt ? jt + (size_t)p * MJ : NULL;
+    d.S = S; d.MJ = jt ? MJ : 0;
+    float x[MAXD];
+    size_t row = (size_t)p * (S + 1);
+    int k = run_path(I, &d, 1, S, paths ? paths + row * D : NULL, left ? left + row * D : NULL,
+                     time ? time + row : NULL, jumps ? jumps + row * D : NULL, NULL, x);
+    if (k < 0) bad = 1;
+    if (steps) steps[p] = k;
+    if (payoffs) payoffs[p] = oracle_payoff(I, x) * I->discount;
+  }
+  return bad ? SDEMC_EOVERFLOW : SDEMC_OK;
+}
+
+/* Re-run paths [0, n) from the raw draws a GPU run exported: z (n, S, zdim),
+ * jump times/marks/picks (n, jcap).  exact selects the Euler op order. */
+int oracle_from_export(const sdemc_inst* I, int64_t n, int S, const float* z, int zdim,
+                       const float* jt, const float* jm, const int32_t* js, int jcap, int exact,
+                       float* paths, float* left, float* time, float* jumps, float* normals,
+                       float* payoffs, int32_t* steps) {
+  const int D = I->dim, NW = nw_of(I->noise);
+  int bad = 0;
+  for (int64_t p = 0; p < n; ++p) {
+    draws_t d;
+    memset(&d, 0, sizeof(d));
+    d.mode = DRAW_EXPORT;
+    d.z = z + (size_t)p * S * zdim; d.zdim = zdim; d.S = S;
+    d.xjt = jt ? jt + (size_t)p * jcap : NULL;
+    d.xjm = jm ? jm + (size_t)p * jcap : NULL;
+    d.xjsel = js ? js + (size_t)p * jcap : NULL;
+    d.jcap = jt ? jcap : 0;
+    d.h_nom = I->h; d.sq_h = sqrtf(I->h);
+    float x[MAXD];
+    size_t row = (size_t)p * (S + 1);
+    int k = run_path(I, &d, exact, S, paths ? paths + row * D : NULL, left ? left + row * D : NULL,
+                     time ? time + row : NULL, jumps ? jumps + row * D : NULL,
+                     normals ? normals + (size_t)p * S * D * NW : NULL, x);
+    if (k < 0) bad = 1;
+    if (steps) steps[p] = k;
+    if (payoffs) payoffs[p] = oracle_payoff(I, x) * I->discount;
+  }
+  return bad ? SDEMC_EOVERFLOW : SDEMC_OK;
+}
+
+/* ------------------------------------------------------------- MLMC ----- */
+static int run_pair(const sdemc_inst* I, draws_t* d, int exact, int factor, float hf0, float hc0,
+                    int cap, float* xf, float* xc) {
+  const int D = I->dim;
+  for (int i = 0; i < D; ++i) { xf[i] = I->x0[i]; xc[i] = I->x0[i]; }
+  const float T = I->T;
+  float tf = 0.f, tc = 0.f, hf = hf0, hc = hc0;
+  float dW[MAXD], dW2[MAXD], sW[MAXD], sW2[MAXD], oldf[MAXD], oldc[MAXD];
+  int kf = 0, kc = 0;
+  if (I->grid == SDEMC_GRID_UNIFORM) {
+    /* DiffusionSolver.multilevel_solve (sde_mc/solvers.py:90-119) */
+    for (kc = 0; kc < I->num_steps; ++kc) {
+      for (int i = 0; i < D; ++i) { sW[i] = 0.f; sW2[i] = 0.f; }
+      for (int sub = 0; sub < factor; ++sub) {
+        draws_increments(I, D, d, kf, hf, dW, dW2);
+        euler(I, D, exact, xf, hf, dW, dW2);
+        for (int i = 0; i < D; ++i) { sW[i] = sW[i] + dW[i]; sW2[i] = sW2[i] + dW2[i]; }
+        ++kf;
+      }
+      euler(I, D, exact, xc, hc, sW, sW2);
+    }
+    return kc;
+  }
+  float nj = draws_jump_first(I, D, d);
+  while (tf < T) {
+    if (kc >= cap) return -1;
+    for (int i = 0; i < D; ++i) { sW[i] = 0.f; sW2[i] = 0.f; }
+    for (int sub = 0; sub < factor; ++sub) {
+      hf = fminf(hf, fmaxf(T - tf, 0.f));
+      float dtf = fminf(hf, nj - tf);
+      draws_increments(I, D, d, kf, dtf, dW, dW2);
+      memcpy(oldf, xf, sizeof(float) * D);
+      euler(I, D, exact, xf, dtf, dW, dW2);
+      tf = tf + dtf;
+      for (int i = 0; i < D; ++i) { sW[i] = sW[i] + dW[i]; sW2[i] = sW2[i] + dW2[i]; }
+      ++kf;
+    }
+    hc = fminf(hc, fmaxf(T - tc, 0.f));
+    float dtc = fminf(hc, nj - tc);
+    memcpy(oldc, xc, sizeof(float) * D);
+    euler(I, D, exact, xc, dtc, sW, sW2);
+    tc = tc + dtc;
+    if (jump_due(nj, tf)) {
+      float J; int sel;
+      draws_jump_mark(d, kc, &J, &sel);
+      apply_jump(I, D, exact, xf, I->exact_jumps ? xf : oldf, J, sel);
+      apply_jump(I, D, exact, xc, I->exact_jumps ? xc : oldc, J, sel);
+      nj = draws_jump_next(I, D, d, nj);
+    }
+    ++kc;
+  }
+  return d->overflow ? -1 : kc;
+}
+
+int oracle_mlmc_replay(const sdemc_inst* I, int factor, float hf, float hc, int bs, int Sf, int Sc,
+                       int MJ, const float* jt, const float* dw, const float* marks,
+                       const int32_t* asset, float* xf, float* xc) {
+  const int D = I->dim, NW = nw_of(I->noise);
+  int bad = 0;
+  for (int p = 0; p < bs; ++p) {
+    draws_t d;
+    memset(&d, 0, sizeof(d));
+    d.mode = DRAW_REPLAY;
+    d.dw = dw + (size_t)p * Sf * D * NW;
+    d.marks = marks ? marks + (size_t)p * Sc : NULL;
+    d.asset = asset ? asset + (size_t)p * Sc : NULL;
+    d.jt = jt ? jt + (size_t)p * MJ : NULL;
+    d.S = Sf; d.MJ = jt ? MJ : 0;
+    if (run_pair(I, &d, 1, factor, hf, hc, Sc, xf + (size_t)p * D, xc + (size_t)p * D) < 0) bad = 1;
+  }
+  return bad ? SDEMC_EOVERFLOW : SDEMC_OK;
+}
+
+/* ------------------------------------------------- native (baseline) ---- */
+typedef struct {
+  const sdemc_inst* I; int64_t p0, p1; int cap; int exact; int mode_mlmc; int factor;
+  float hf, hc; double s, s2, f, f2; int64_t n; int bad; float* payoffs;
+} job_t;
+
+static void* job_run(void* arg) {
+  job_t* j = (job_t*)arg;
+  const sdemc_inst* I = j->I;
+  float x[MAXD], xc[MAXD];
+  for (int64_t p = j->p0; p < j->p1; ++p) {
+    draws_t d;
+    draws_native_init(I, &d, p);
+    if (j->mode_mlmc) {
+      if (run_pair(I, &d, j->exact, j->factor, j->hf, j->hc, j->cap, x, xc) < 0) j->bad = 1;
+      float pf = oracle_payoff(I, x), pc = oracle_payoff(I, xc);
+      float y = I->discount * (pf - pc), f = pf * I->discount;
+      j->s += y; j->s2 += (double)y * y; j->f += f; j->f2 += (double)f * f;
+      if (j->payoffs) j->payoffs[p] = y;
+    } else {
+      if (run_path(I, &d, j->exact, j->cap, NULL, NULL, NULL, NULL, NULL, x) < 0) j->bad = 1;
+      float P = oracle_payoff(I, x) * I->discount;
+      j->s += P; j->s2 += (double)P * P;
+      if (j->payoffs) j->payoffs[p] = P;
+    }
+    j->n++;
+  }
+  return NULL;
+}
+
+static int run_jobs(const sdemc_inst* I, int nthreads, int mlmc, int factor, float hf, float hc,
+                    float* payoffs, double* out) {
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > 256) nthreads = 256;
+  job_t jobs[256];
+  pthread_t th[256];
+  const int64_t N = I->num_paths;
+  const double lam = (double)I->rate * I->T;
+  const int cap = I->num_steps + (int)(2.0 * (lam + 12.0 * sqrt(lam > 1 ? lam : 1) + 64.0)) + 8;
+  for (int t = 0; t < nthreads; ++t) {
+    memset(&jobs[t], 0, sizeof(job_t));
+    jobs[t].I = I; jobs[t].p0 = N * t / nthreads; jobs[t].p1 = N * (t + 1) / nthreads;
+    jobs[t].cap = cap; jobs[t].exact = 0; jobs[t].mode_mlmc = mlmc; jobs[t].factor = factor;
+    jobs[t].hf = hf; jobs[t].hc = hc; jobs[t].payoffs = payoffs;
+    pthread_create(&th[t], NULL, job_run, &jobs[t]);
+  }
+  double s = 0, s2 = 0, f = 0, f2 = 0;
+  int64_t n = 0;
+  int bad = 0;
+  for (int t = 0; t < nthreads; ++t) {
+    pthread_join(th[t], NULL);
+    s += jobs[t].s; s2 += jobs[t].s2; f += jobs[t].f; f2 += jobs[t].f2; n += jobs[t].n; bad |= jobs[t].bad;
+  }
+  out[0] = s; out[1] = s2; out[2] = (double)n;
+  out[3] = n > 0 ? s / n : 0.0;
+  out[4] = n > 1 ? (s2 - s * s / n) / (n - 1.0) : 0.0;
+  out[5] = f; out[6] = f2;
+  return bad ? SDEMC_EOVERFLOW : SDEMC_OK;
+}
+
+/* Price num_paths paths natively: out = (sum, sum_sq, n, mean, var, -, -). */
+int oracle_price(const sdemc_inst* I, int nthreads, float* payoffs, double* out) {
+  return run_jobs(I, nthreads, 0, 1, 0.f, 0.f, payoffs, out);
+}
+
+/* One MLMC level natively: out = (sumY, sumY2, n, mean, var, sumPf, sumPf2). */
+int oracle_mlmc_level(const sdemc_inst* I, int factor, float hf, float hc, int nthreads, float* ys,
+                      double* out) {
+  return run_jobs(I, nthreads, 1, factor, hf, hc, ys, out);
+}
+
+/* The GPU's reduction order, restated: FP32 lane sums over 4 rounds, an xor
+ * butterfly over 32 lanes per chunk of 128 paths, FP64 chunk partials, then
+ * 256 strided FP64 accumulators and a halving tree.  width 3 (price) or 5
+ * (MLMC: vals2 holds the second payoff series). out = sums..., mean, var. */
+void oracle_chunk_reduce(const float* vals, const float* vals2, int64_t n, double* out) {
+  const int64_t nch = (n + SDEMC_CHUNK_PATHS - 1) / SDEMC_CHUNK_PATHS;
+  const int width = vals2 ? 5 : 3;
+  double acc[256][5];
+  memset(acc, 0, sizeof(acc));
+  for (int64_t c = 0; c < nch; ++c) {
+    float ls[32], ls2[32], lf[32], lf2[32];
+    int cnt = 0;
+    for (int l = 0; l < 32; ++l) {
+      ls[l] = 0.f; ls2[l] = 0.f; lf[l] = 0.f; lf2[l] = 0.f;
+      for (int r = 0; r < 4; ++r) {
+        int64_t p = c * 128 + r * 32 + l;
+        if (p < n) {
+          float v = vals[p];
+          ls[l] = ls[l] + v; ls2[l] = ls2[l] + v * v;
+          if (vals2) { float w = vals2[p]; lf[l] = lf[l] + w; lf2[l] = lf2[l] + w * w; }
+          ++cnt;
+        }
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      float a[32], b[32], e[32], g[32];
+      for (int l = 0; l < 32; ++l) {
+        a[l] = ls[l] + ls[l ^ o]; b[l] = ls2[l] + ls2[l ^ o];
+        e[l] = lf[l] + lf[l ^ o]; g[l] = lf2[l] + lf2[l ^ o];
+      }
+      memcpy(ls, a, sizeof(a)); memcpy(ls2, b, sizeof(b)); memcpy(lf, e, sizeof(e)); memcpy(lf2, g, sizeof(g));
+    }
+    double row[5] = {(double)ls[0], (double)ls2[0], (double)cnt, (double)lf[0], (double)lf2[0]};
+    int tid = (int)(c % 256);
+    for (int w = 0; w < width; ++w) acc[tid][w] += row[w];
+  }
+  for (int o = 128; o > 0; o >>= 1)
+    for (int i = 0; i < o; ++i)
+      for (int w = 0; w < width; ++w) acc[i][w] += acc[i + o][w];
+  for (int w = 0; w < width; ++w) out[w] = acc[0][w];
+  double s = acc[0][0], s2 = acc[0][1], m = acc[0][2];
+  out[width] = m > 0 ? s / m : 0.0;
+  out[width + 1] = m > 1 ? (s2 - s * s / m) / (m - 1.0) : 0.0;
+}

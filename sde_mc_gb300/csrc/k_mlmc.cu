@@ -1,0 +1,277 @@
+// k_mlmc.cu — K2: one multilevel Monte Carlo level in one launch.
+//
+// JumpDiffusionSolver.multilevel_solve (sde_mc/solvers.py:228-307) couples a
+// fine path (h_f) and a coarse path (h_c = factor * h_f) through one jump
+// clock: each coarse step is `factor` fine sub-steps whose increments it sums,
+// both levels get the same mark, and after a jump the remaining fine sub-steps
+// have dt = 0.  Here the fine and coarse states of a path live in the same
+// thread, the sub-step increments are drawn once, and the level's
+// sum/sum-of-squares of Y = disc*(P_f - P_c) (sde_mc/mlmc.py:59-69) are reduced
+// as in K1.  The replay twin runs the same loop on recorded draws.
+#include "sdemc_device.cuh"
+#include "sdemc_host.cuh"
+
+namespace sdemc {
+
+template <int D, int NOISE, bool EXACT, class Draws>
+SDEMC_DI void simulate_pair(const sdemc_inst& I, Draws& dr, int factor, float hf0, float hc0,
+                            float* xf, float* xc, int max_iters, bool& overflow) {
+  using L = Layout<D, NOISE>;
+#pragma unroll
+  for (int i = 0; i < D; ++i) { xf[i] = I.x0[i]; xc[i] = I.x0[i]; }
+  const float T = I.T;
+  float tf = 0.f, tc = 0.f, hf = hf0, hc = hc0;
+  float dW[D], dW2[D], z[L::ZD], sW[D], sW2[D], oldf[D], oldc[D];
+#pragma unroll
+  for (int i = 0; i < D; ++i) { dW2[i] = 0.f; oldf[i] = xf[i]; }
+  int kf = 0, kc = 0;
+  if (I.grid == SDEMC_GRID_UNIFORM) {
+    // DiffusionSolver.multilevel_solve (sde_mc/solvers.py:90-119): `coarse`
+    // blocks of `factor` fine steps of h_f, then one coarse step of h_c driven
+    // by the summed increments; no time checks.
+    const int coarse = I.num_steps;
+    for (kc = 0; kc < coarse; ++kc) {
+#pragma unroll
+      for (int i = 0; i < D; ++i) { sW[i] = 0.f; sW2[i] = 0.f; }
+      for (int sub = 0; sub < factor; ++sub) {
+        dr.increments(I, kf, hf, dW, dW2, z);
+        euler<D, NOISE, EXACT>(I, xf, hf, dW, dW2);
+#pragma unroll
+        for (int i = 0; i < D; ++i) { sW[i] = __fadd_rn(sW[i], dW[i]); sW2[i] = __fadd_rn(sW2[i], dW2[i]); }
+        ++kf;
+      }
+      euler<D, NOISE, EXACT>(I, xc, hc, sW, sW2);
+    }
+    return;
+  }
+  float nj = dr.jump_first(I);
+  bool act = tf < T;
+  while (__any_sync(kFull, act)) {
+    if (kc >= max_iters) { overflow = true; break; }
+#pragma unroll
+    for (int i = 0; i < D; ++i) { sW[i] = 0.f; sW2[i] = 0.f; }
+    for (int sub = 0; sub < factor; ++sub) {
+      hf = fminf(hf, fmaxf(__fsub_rn(T, tf), 0.f));
+      float dtf = fminf(hf, __fsub_rn(nj, tf));
+      if (!act) dtf = 0.f;
+      dr.increments(I, kf, dtf, dW, dW2, z);
+#pragma unroll
+      for (int i = 0; i < D; ++i) oldf[i] = xf[i];
+      euler<D, NOISE, EXACT>(I, xf, dtf, dW, dW2);
+      tf = __fadd_rn(tf, dtf);
+#pragma unroll
+      for (int i = 0; i < D; ++i) { sW[i] = __fadd_rn(sW[i], dW[i]); sW2[i] = __fadd_rn(sW2[i], dW2[i]); }
+      ++kf;
+    }
+    hc = fminf(hc, fmaxf(__fsub_rn(T, tc), 0.f));
+    float dtc = fminf(hc, __fsub_rn(nj, tc));
+    if (!act) dtc = 0.f;
+#pragma unroll
+    for (int i = 0; i < D; ++i) oldc[i] = xc[i];
+    euler<D, NOISE, EXACT>(I, xc, dtc, sW, sW2);
+    tc = __fadd_rn(tc, dtc);
+    if (act && jump_due(nj, tf)) {
+      float J;
+      int sel;
+      dr.jump_mark(kc, J, sel);
+      apply_jump<D, EXACT>(I, xf, I.exact_jumps ? xf : oldf, J, sel);
+      apply_jump<D, EXACT>(I, xc, I.exact_jumps ? xc : oldc, J, sel);
+      nj = dr.jump_next(I, nj);
+    }
+    ++kc;
+    act = tf < T;
+  }
+}
+
+template <int D, int NOISE>
+__global__ void __launch_bounds__(128)
+mlmc_kernel(const __grid_constant__ sdemc_inst I, int factor, float hf, float hc,
+            double* __restrict__ part, float* __restrict__ yout, int32_t* __restrict__ status,
+            int64_t nchunks, int max_iters) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  bool ovf = false;
+  for (int64_t c = warp; c < nchunks; c += nwarps) {
+    float s = 0.f, s2 = 0.f, f = 0.f, f2 = 0.f;
+    int n = 0;
+#pragma unroll 1
+    for (int r = 0; r < kChunk / 32; ++r) {
+      const int64_t p = c * kChunk + r * 32 + lane;
+      NativeDraws<D, NOISE> dr;
+      dr.init(I, (uint64_t)p);
+      float xf[D], xc[D];
+      simulate_pair<D, NOISE, false>(I, dr, factor, hf, hc, xf, xc, max_iters, ovf);
+      const float pf = payoff<D>(I, xf), pc = payoff<D>(I, xc);
+      const float Y = __fmul_rn(I.discount, __fsub_rn(pf, pc));
+      const float F = __fmul_rn(pf, I.discount);
+      if (p < I.num_paths) {
+        s = __fadd_rn(s, Y);
+        s2 = __fadd_rn(s2, __fmul_rn(Y, Y));
+        f = __fadd_rn(f, F);
+        f2 = __fadd_rn(f2, __fmul_rn(F, F));
+        ++n;
+        if (yout) yout[p] = Y;
+      }
+    }
+    s = warp_sum(s); s2 = warp_sum(s2); f = warp_sum(f); f2 = warp_sum(f2);
+    n = __reduce_add_sync(kFull, n);
+    if (lane == 0) {
+      double* o = part + c * 5;
+      o[0] = (double)s; o[1] = (double)s2; o[2] = (double)n; o[3] = (double)f; o[4] = (double)f2;
+    }
+  }
+  if (ovf) atomicOr(status, SDEMC_EOVERFLOW);
+}
+
+template <int D, int NOISE>
+__global__ void __launch_bounds__(128)
+mlmc_replay_kernel(const __grid_constant__ sdemc_inst I, int factor, float hf, float hc, int bs,
+                   int Sf, int Sc, int MJ, const float* jt, const float* dw, const float* marks,
+                   const int32_t* asset, float* xf_out, float* xc_out, int32_t* status) {
+  using L = Layout<D, NOISE>;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = p < bs;
+  ReplayDraws<D, NOISE> dr{};
+  if (valid) {
+    dr.dw = dw + (size_t)p * Sf * D * L::NW;
+    dr.marks = marks ? marks + (size_t)p * Sc : nullptr;
+    dr.asset = asset ? asset + (size_t)p * Sc : nullptr;
+    dr.jt = jt ? jt + (size_t)p * MJ : nullptr;
+    dr.S = Sf;
+    dr.MJ = jt ? MJ : 0;
+  }
+  bool ovf = false;
+  float xf[D], xc[D];
+  simulate_pair<D, NOISE, true>(I, dr, factor, hf, hc, xf, xc, Sc, ovf);
+  if (!valid) return;
+#pragma unroll
+  for (int i = 0; i < D; ++i) { xf_out[(size_t)p * D + i] = xf[i]; xc_out[(size_t)p * D + i] = xc[i]; }
+  if (ovf || dr.overflow) atomicOr(status, SDEMC_EOVERFLOW);
+}
+
+template <int D, int NOISE>
+__global__ void __launch_bounds__(128)
+mlmc_terminals_kernel(const __grid_constant__ sdemc_inst I, int factor, float hf, float hc,
+                      float* xf_out, float* xc_out, int32_t* status, int max_iters) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  NativeDraws<D, NOISE> dr;
+  dr.init(I, (uint64_t)p);
+  bool ovf = false;
+  float xf[D], xc[D];
+  simulate_pair<D, NOISE, false>(I, dr, factor, hf, hc, xf, xc, max_iters, ovf);
+  if (p >= I.num_paths) return;
+#pragma unroll
+  for (int i = 0; i < D; ++i) { xf_out[p * D + i] = xf[i]; xc_out[p * D + i] = xc[i]; }
+  if (ovf) atomicOr(status, SDEMC_EOVERFLOW);
+}
+
+static int check_levels(const sdemc_inst* I, int fine, int coarse, float hf, float hc) {
+  if (fine < 1 || coarse < 1 || fine % coarse != 0)
+    return fail(SDEMC_EINVAL, "levels (%d, %d): fine must be a multiple of coarse", fine, coarse);
+  if (!(hf > 0.f) || !(hc > 0.f)) return fail(SDEMC_EINVAL, "non-positive level steps");
+  if (I->grid == SDEMC_GRID_ADAPTED && I->noise == SDEMC_NOISE_INDEP_PAIR)
+    return fail(SDEMC_EUNSUPPORTED, "paired noise on the adapted grid");
+  return SDEMC_OK;
+}
+
+}  // namespace sdemc
+
+using namespace sdemc;
+
+extern "C" size_t sdemc_mlmc_scratch_bytes(const sdemc_inst* h_inst) {
+  if (!h_inst) return 0;
+  return kScratchHeader + (size_t)num_chunks(h_inst) * 5 * sizeof(double);
+}
+
+extern "C" int sdemc_mlmc_level(const sdemc_inst* h_inst, int fine, int coarse, float h_fine,
+                                float h_coarse, const sdemc_cfg* h_cfg, void* d_scratch,
+                                size_t scratch_bytes, double* d_out, float* d_y, void* stream) {
+  int rc = validate_inst(h_inst);
+  if (rc) return rc;
+  if ((rc = check_levels(h_inst, fine, coarse, h_fine, h_coarse))) return rc;
+  if (!d_scratch || !d_out) return fail(SDEMC_EINVAL, "null scratch or output");
+  if (scratch_bytes < sdemc_mlmc_scratch_bytes(h_inst))
+    return fail(SDEMC_ENOMEM, "scratch %zu bytes < required %zu", scratch_bytes,
+                sdemc_mlmc_scratch_bytes(h_inst));
+  sdemc_cfg cfg{};
+  if (h_cfg) cfg = *h_cfg;
+  sdemc_inst I = *h_inst;
+  I.num_steps = coarse;  // iteration cap counts coarse steps
+  cudaStream_t s = (cudaStream_t)stream;
+  int32_t* status = (int32_t*)d_scratch;
+  double* part = (double*)((char*)d_scratch + kScratchHeader);
+  const int64_t nch = num_chunks(h_inst);
+  const int factor = fine / coarse;
+  const int mi = max_iterations(&I);
+  if (nch > 0) {
+    const int threads = cfg.block_threads > 0 ? cfg.block_threads : 128;
+#define SDEMC_MLMC_CASE(D_, N_)                                                                  \
+  {                                                                                              \
+    auto kern = mlmc_kernel<D_, N_>;                                                             \
+    int per_sm = 0;                                                                              \
+    if ((rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0), \
+                         "occupancy query")))                                                    \
+      return rc;                                                                                 \
+    if (cfg.ctas_per_sm > 0 && cfg.ctas_per_sm < per_sm) per_sm = cfg.ctas_per_sm;               \
+    if (per_sm < 1) per_sm = 1;                                                                  \
+    int64_t ctas = (nch + threads / 32 - 1) / (threads / 32);                                    \
+    const int64_t resident = (int64_t)num_sms() * per_sm;                                        \
+    if (ctas > resident) ctas = resident;                                                        \
+    kern<<<(unsigned)ctas, threads, 0, s>>>(I, factor, h_fine, h_coarse, part, d_y, status, nch, mi); \
+  }
+    SDEMC_DISPATCH(I.dim, I.noise, SDEMC_MLMC_CASE)
+#undef SDEMC_MLMC_CASE
+    if ((rc = check_cuda(cudaGetLastError(), "mlmc_kernel launch"))) return rc;
+  }
+  return launch_reduce(part, nch, 5, status, d_out, s);
+}
+
+extern "C" int sdemc_mlmc_replay(const sdemc_inst* h_inst, int fine, int coarse, float h_fine,
+                                 float h_coarse, int bs, int fine_cap, int coarse_cap,
+                                 int max_jumps, const float* d_jump_times, const float* d_dw,
+                                 const float* d_marks, const int32_t* d_asset, float* d_xf,
+                                 float* d_xc, int32_t* d_status, void* stream) {
+  int rc = validate_inst(h_inst);
+  if (rc) return rc;
+  if ((rc = check_levels(h_inst, fine, coarse, h_fine, h_coarse))) return rc;
+  if (bs < 0 || fine_cap < 1 || coarse_cap < 1) return fail(SDEMC_EINVAL, "bad replay shape");
+  if (!d_dw || !d_xf || !d_xc || !d_status) return fail(SDEMC_EINVAL, "null replay buffer");
+  if (h_inst->rate > 0.f && (!d_jump_times || !d_marks || max_jumps < 1))
+    return fail(SDEMC_EINVAL, "jump replay needs jump times and marks");
+  if (bs == 0) return SDEMC_OK;
+  sdemc_inst I = *h_inst;
+  I.num_steps = coarse;
+  cudaStream_t s = (cudaStream_t)stream;
+  const unsigned blocks = (unsigned)((bs + 127) / 128);
+  const int factor = fine / coarse;
+#define SDEMC_MLMC_REPLAY_CASE(D_, N_)                                                        \
+  mlmc_replay_kernel<D_, N_><<<blocks, 128, 0, s>>>(I, factor, h_fine, h_coarse, bs, fine_cap, \
+                                                    coarse_cap, max_jumps, d_jump_times, d_dw, \
+                                                    d_marks, d_asset, d_xf, d_xc, d_status);
+  SDEMC_DISPATCH(I.dim, I.noise, SDEMC_MLMC_REPLAY_CASE)
+#undef SDEMC_MLMC_REPLAY_CASE
+  return check_cuda(cudaGetLastError(), "mlmc_replay_kernel launch");
+}
+
+extern "C" int sdemc_mlmc_terminals(const sdemc_inst* h_inst, int fine, int coarse, float h_fine,
+                                    float h_coarse, float* d_xf, float* d_xc, int32_t* d_status,
+                                    void* stream) {
+  int rc = validate_inst(h_inst);
+  if (rc) return rc;
+  if ((rc = check_levels(h_inst, fine, coarse, h_fine, h_coarse))) return rc;
+  if (!d_xf || !d_xc || !d_status) return fail(SDEMC_EINVAL, "null output");
+  if (h_inst->num_paths == 0) return SDEMC_OK;
+  sdemc_inst I = *h_inst;
+  I.num_steps = coarse;
+  cudaStream_t s = (cudaStream_t)stream;
+  const unsigned blocks = (unsigned)((I.num_paths + 127) / 128);
+  const int factor = fine / coarse;
+  const int mi = max_iterations(&I);
+#define SDEMC_MLMC_TERM_CASE(D_, N_)                                               \
+  mlmc_terminals_kernel<D_, N_><<<blocks, 128, 0, s>>>(I, factor, h_fine, h_coarse, \
+                                                       d_xf, d_xc, d_status, mi);
+  SDEMC_DISPATCH(I.dim, I.noise, SDEMC_MLMC_TERM_CASE)
+#undef SDEMC_MLMC_TERM_CASE
+  return check_cuda(cudaGetLastError(), "mlmc_terminals_kernel launch");
+}

@@ -1,0 +1,126 @@
+// k_price.cu — K1: fused path simulation + payoff + reduction.
+//
+// Stands in for mc_simple (sde_mc/mc.py:53-123) driving JumpDiffusionSolver
+// .solve (sde_mc/solvers.py:164-226) or DiffusionSolver.solve (:68-88) and
+// Option.__call__ (sde_mc/options.py:175-176).  Nothing path-shaped touches
+// HBM: each lane keeps its path in registers, draws its increments from its
+// own Philox stream, and folds its discounted payoff into FP32 lane sums.
+// A chunk of SDEMC_CHUNK_PATHS consecutive paths (32 lanes x 4 rounds) is
+// reduced by a fixed warp butterfly and stored as (sum, sum_sq, n) in FP64 at
+// its own slot, so the bits never depend on the grid shape.
+#include "sdemc_device.cuh"
+#include "sdemc_host.cuh"
+
+namespace sdemc {
+
+template <int D, int NOISE, bool EXACT>
+__global__ void __launch_bounds__(256)
+price_kernel(const __grid_constant__ sdemc_inst I, double* __restrict__ part,
+             float* __restrict__ payoffs, int32_t* __restrict__ status,
+             int64_t nchunks, int max_iters) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  bool ovf = false;
+  for (int64_t c = warp; c < nchunks; c += nwarps) {
+    float s = 0.f, s2 = 0.f;
+    int n = 0;
+#pragma unroll 1
+    for (int r = 0; r < kChunk / 32; ++r) {
+      const int64_t p = c * kChunk + r * 32 + lane;
+      NativeDraws<D, NOISE> dr;
+      dr.init(I, (uint64_t)p);
+      NullSink sk;
+      float x[D];
+      simulate<D, NOISE, EXACT>(I, dr, sk, x, max_iters, ovf);
+      const float P = __fmul_rn(payoff<D>(I, x), I.discount);
+      if (p < I.num_paths) {
+        s = __fadd_rn(s, P);
+        s2 = __fadd_rn(s2, __fmul_rn(P, P));
+        ++n;
+        if (payoffs) payoffs[p] = P;
+      }
+    }
+    s = warp_sum(s);
+    s2 = warp_sum(s2);
+    n = __reduce_add_sync(kFull, n);
+    if (lane == 0) {
+      part[c * 3 + 0] = (double)s;
+      part[c * 3 + 1] = (double)s2;
+      part[c * 3 + 2] = (double)n;
+    }
+  }
+  if (ovf) atomicOr(status, SDEMC_EOVERFLOW);
+}
+
+template <int D, int NOISE, bool EXACT>
+static int launch_price_t(const sdemc_inst& I, const sdemc_cfg& cfg, double* part,
+                          float* payoffs, int32_t* status, int64_t nchunks, cudaStream_t s) {
+  auto kern = price_kernel<D, NOISE, EXACT>;
+  const int threads = cfg.block_threads > 0 ? cfg.block_threads : 128;
+  int per_sm = 0;
+  int rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0),
+                      "occupancy query");
+  if (rc) return rc;
+  if (cfg.ctas_per_sm > 0 && cfg.ctas_per_sm < per_sm) per_sm = cfg.ctas_per_sm;
+  if (per_sm < 1) per_sm = 1;
+  const int64_t resident = (int64_t)num_sms() * per_sm;
+  const int64_t warps_per_cta = threads / 32;
+  int64_t ctas = (nchunks + warps_per_cta - 1) / warps_per_cta;
+  if (ctas > resident) ctas = resident;
+  if (ctas < 1) ctas = 1;
+  kern<<<(unsigned)ctas, threads, 0, s>>>(I, part, payoffs, status, nchunks, max_iterations(&I));
+  return check_cuda(cudaGetLastError(), "price_kernel launch");
+}
+
+}  // namespace sdemc
+
+using namespace sdemc;
+
+extern "C" size_t sdemc_price_scratch_bytes(const sdemc_inst* h_inst) {
+  if (!h_inst) return 0;
+  return kScratchHeader + (size_t)num_chunks(h_inst) * 3 * sizeof(double);
+}
+
+extern "C" int sdemc_price_chunks(const sdemc_inst* h_inst, const sdemc_cfg* h_cfg, void* d_scratch,
+                                  size_t scratch_bytes, float* d_payoffs, void* stream) {
+  int rc = validate_inst(h_inst);
+  if (rc) return rc;
+  if (!d_scratch) return fail(SDEMC_EINVAL, "null scratch");
+  if (scratch_bytes < sdemc_price_scratch_bytes(h_inst))
+    return fail(SDEMC_ENOMEM, "scratch %zu bytes < required %zu", scratch_bytes,
+                sdemc_price_scratch_bytes(h_inst));
+  if (h_cfg && h_cfg->block_threads % 32 != 0)
+    return fail(SDEMC_EINVAL, "block_threads %d not a multiple of 32", h_cfg->block_threads);
+  sdemc_cfg cfg{};
+  if (h_cfg) cfg = *h_cfg;
+  const sdemc_inst& I = *h_inst;
+  cudaStream_t s = (cudaStream_t)stream;
+  int32_t* status = (int32_t*)d_scratch;
+  double* part = (double*)((char*)d_scratch + kScratchHeader);
+  const int64_t nch = num_chunks(h_inst);
+  if (nch == 0) return SDEMC_OK;
+  const bool exact = (cfg.flags & SDEMC_CFG_EXACT_EULER) != 0;
+#define SDEMC_PRICE_CASE(D_, N_)                                                              \
+  rc = exact ? launch_price_t<D_, N_, true>(I, cfg, part, d_payoffs, status, nch, s)          \
+             : launch_price_t<D_, N_, false>(I, cfg, part, d_payoffs, status, nch, s);
+  SDEMC_DISPATCH(I.dim, I.noise, SDEMC_PRICE_CASE)
+#undef SDEMC_PRICE_CASE
+  return rc;
+}
+
+extern "C" int sdemc_reduce_chunks(void* d_scratch, int64_t nchunks, int width, double* d_out,
+                                   void* stream) {
+  if (!d_scratch || !d_out || nchunks < 0) return fail(SDEMC_EINVAL, "bad reduce args");
+  int32_t* status = (int32_t*)d_scratch;
+  double* part = (double*)((char*)d_scratch + kScratchHeader);
+  return launch_reduce(part, nchunks, width, status, d_out, (cudaStream_t)stream);
+}
+
+extern "C" int sdemc_price(const sdemc_inst* h_inst, const sdemc_cfg* h_cfg, void* d_scratch,
+                           size_t scratch_bytes, double* d_out, float* d_payoffs, void* stream) {
+  if (!d_out) return fail(SDEMC_EINVAL, "null output");
+  int rc = sdemc_price_chunks(h_inst, h_cfg, d_scratch, scratch_bytes, d_payoffs, stream);
+  if (rc) return rc;
+  return sdemc_reduce_chunks(d_scratch, num_chunks(h_inst), 3, d_out, stream);
+}

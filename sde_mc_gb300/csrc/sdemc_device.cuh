@@ -1,0 +1,509 @@
+// sdemc_device.cuh — device building blocks shared by every path kernel.
+//
+//  * Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as
+//    easy as 1, 2, 3", SC'11), written from the paper; counter-based, so any
+//    path's draws are a pure function of (seed, stream, path index, block).
+//  * Box-Muller normals on MUFU intrinsics (__logf, rsqrtf, __sinf/__cosf).
+//  * The reference's jump-adapted Euler loop (sde_mc/solvers.py:164-226) with
+//    its exact float32 grid arithmetic, written with _rn intrinsics so that no
+//    multiply-add contraction changes a rounding the reference does not make.
+//  * Payoffs of sde_mc/options.py:167-321.
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+#include "../../include/sdemc.h"
+
+namespace sdemc {
+
+#define SDEMC_DI __device__ __forceinline__
+constexpr unsigned kFull = 0xffffffffu;
+constexpr float kTwoPi = 6.283185307179586f;
+constexpr float kPi = 3.141592653589793f;
+
+// ---------------------------------------------------------------- Philox ----
+struct U4 { uint32_t x, y, z, w; };
+
+SDEMC_DI U4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                          uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+    const uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
+    const uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
+    const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+  }
+  return U4{c0, c1, c2, c3};
+}
+
+// Uniform on (0,1): (2m+1) 2^-24 from the top 23 bits m of w (exact, never 0/1).
+SDEMC_DI float u01(uint32_t w) {
+  return __fsub_rn(__uint_as_float(0x3F800000u | (w >> 9)), 0.99999994f);
+}
+
+// Box-Muller pair: r = sqrt(-2 ln ua), th = 2 pi ub - pi.
+SDEMC_DI float bm_radius(uint32_t wa) {
+  const float e = -2.0f * __logf(u01(wa));
+  return e * rsqrtf(e);
+}
+SDEMC_DI float bm_angle(uint32_t wb) { return __fmaf_rn(kTwoPi, u01(wb), -kPi); }
+
+// Stream tags (counter word c2 high half).
+constexpr uint32_t kTagDiffusion = 0u;
+constexpr uint32_t kTagJumps = 1u;
+
+struct StreamKey {
+  uint32_t k0, k1, c1, c2base, c3;
+  SDEMC_DI void init(uint64_t seed, uint32_t stream_id, uint64_t gpath) {
+    k0 = (uint32_t)seed; k1 = (uint32_t)(seed >> 32);
+    c1 = (uint32_t)gpath; c2base = (uint32_t)(gpath >> 32) & 0xFFFFu;
+    c3 = stream_id;
+  }
+  SDEMC_DI U4 block(uint32_t tag, uint32_t b) const {
+    return philox4x32_10(b, c1, c2base | (tag << 16), c3, k0, k1);
+  }
+};
+
+// ------------------------------------------------------------- layouts -----
+template <int D, int NOISE> struct Layout {
+  // normals per step drawn from the diffusion stream
+  static constexpr int ZD = NOISE == SDEMC_NOISE_DIAG ? D
+                          : NOISE == SDEMC_NOISE_INDEP_SHARED ? D + 1 : 2 * D;
+  // slots per step: tight when ZD divides 4, else whole Philox blocks
+  static constexpr int SLOTS = (ZD == 1 || ZD == 2 || ZD == 4) ? ZD : 4 * ((ZD + 3) / 4);
+  static constexpr int NB = (ZD + 3) / 4;                 // blocks per step (ZD>2)
+  static constexpr int NW = NOISE == SDEMC_NOISE_DIAG ? 1 : 2;  // noise columns
+};
+
+SDEMC_DI float chol_at(const sdemc_inst& I, int i, int j) { return I.chol[i * (i + 1) / 2 + j]; }
+
+// dW = L (z * sq), evaluated as the oracle mirrors it: zs_j = z_j*sq, then a
+// multiply-add chain over j = 0..i.  For d == 1 the reference's L = [[1.]].
+template <int D>
+SDEMC_DI void correlate(const sdemc_inst& I, const float* z, float sq, float* dW) {
+  float zs[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) zs[j] = __fmul_rn(z[j], sq);
+  if (D == 1) { dW[0] = zs[0]; return; }
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    float acc = __fmul_rn(chol_at(I, i, 0), zs[0]);
+#pragma unroll
+    for (int j = 1; j <= i; ++j) acc = __fmaf_rn(chol_at(I, i, j), zs[j], acc);
+    dW[i] = acc;
+  }
+}
+
+// ------------------------------------------------------------- draws -------
+// Native draws: counter-based Philox streams of one path.
+template <int D, int NOISE>
+struct NativeDraws {
+  using L = Layout<D, NOISE>;
+  StreamKey key;
+  float buf[4];        // buffered normals when ZD in {1,2}
+  uint32_t jblock;     // jump-stream block of the pending jump
+  float jmark;         // mark of the pending jump
+  int jsel;            // asset of the pending jump (ONE_ASSET)
+  float sq_h, h_nom;   // cached sqrt of the nominal step
+
+  SDEMC_DI void init(const sdemc_inst& I, uint64_t gpath) {
+    key.init(I.seed, I.stream_id, I.path_offset + gpath);
+    h_nom = I.h; sq_h = sqrtf(I.h);
+  }
+
+  SDEMC_DI void fill4(uint32_t b, float* o) const {
+    const U4 w = key.block(kTagDiffusion, b);
+    const float r0 = bm_radius(w.x), a0 = bm_angle(w.y);
+    const float r1 = bm_radius(w.z), a1 = bm_angle(w.w);
+    o[0] = r0 * __cosf(a0); o[1] = r0 * __sinf(a0);
+    o[2] = r1 * __cosf(a1); o[3] = r1 * __sinf(a1);
+  }
+
+  // Raw standard normals of step k (k is warp-uniform in lock-step loops).
+  SDEMC_DI void normals(int k, float* z) {
+    constexpr int ZD = L::ZD;
+    if (ZD == 1 || ZD == 2) {
+      const int pos = (k * ZD) & 3;
+      if (pos == 0) fill4((uint32_t)((k * ZD) >> 2), buf);
+      if (ZD == 1) {
+        z[0] = buf[0]; buf[0] = buf[1]; buf[1] = buf[2]; buf[2] = buf[3];
+      } else {
+        z[0] = buf[0]; z[1] = buf[1]; buf[0] = buf[2]; buf[1] = buf[3];
+      }
+    } else {
+#pragma unroll
+      for (int b = 0; b < L::NB; ++b) {
+        float o[4];
+        fill4((uint32_t)(k * L::NB + b), o);
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (4 * b + q < ZD) z[4 * b + q] = o[q];
+      }
+    }
+  }
+
+  // Step increments for step k of length dt.
+  SDEMC_DI void increments(const sdemc_inst& I, int k, float dt, float* dW, float* dW2, float* z) {
+    normals(k, z);
+    const float sq = (dt == h_nom) ? sq_h : sqrtf(dt);
+    correlate<D>(I, z, sq, dW);
+    if (NOISE == SDEMC_NOISE_INDEP_SHARED) {
+      const float s = __fmul_rn(z[D], sq);
+#pragma unroll
+      for (int i = 0; i < D; ++i) dW2[i] = s;
+    } else if (NOISE == SDEMC_NOISE_INDEP_PAIR) {
+      correlate<D>(I, z + D, sq, dW2);
+    }
+  }
+
+  // Jump stream block j: x -> exponential gap, (y, z) -> lognormal mark or the
+  // inverse-CDF uniform, w -> asset pick.
+  SDEMC_DI float load_jump(const sdemc_inst& I, uint32_t j) {
+    const U4 w = key.block(kTagJumps, j);
+    const float gap = -logf(u01(w.x)) * I.inv_rate;
+    if (I.mark == SDEMC_MARK_LOGNORMAL) {
+      const float zn = bm_radius(w.y) * __cosf(bm_angle(w.z));
+      jmark = expf(I.mark_p[1] * zn + I.mark_p[0]) - 1.0f;
+    } else if (I.mark == SDEMC_MARK_INVCDF) {
+      jmark = inverse_cdf(I, u01(w.y) + I.mark_p[9]);
+    } else {
+      jmark = 0.f;
+    }
+    jsel = 0;
+    if (I.jump_target == SDEMC_JUMP_ONE_ASSET) {
+      const float us = u01(w.w);
+#pragma unroll
+      for (int i = 0; i < D - 1; ++i) jsel += (us >= I.jump_cdf[i]) ? 1 : 0;
+    }
+    return gap;
+  }
+
+  // InverseCdf.__call__ (sde_mc/levy.py:22-30): piecewise inverse of the
+  // truncated two-sided tempered-stable jump measure.  mark_p = cm, cp, mu,
+  // alpha, eps, lda, y1, y2, y3, shift, eps^-alpha, -1/alpha.
+  static SDEMC_DI float inverse_cdf(const sdemc_inst& I, float y) {
+    const float cm = I.mark_p[0], cp = I.mark_p[1], mu = I.mark_p[2], al = I.mark_p[3];
+    const float lda = I.mark_p[5], y1 = I.mark_p[6], y2 = I.mark_p[7], y3 = I.mark_p[8];
+    const float epa = I.mark_p[10], nia = I.mark_p[11];
+    if (y <= y1) return logf((mu * lda * y) / cm) / mu - 1.0f;
+    if (y < y2) return -powf(al * ((lda * y / cm) - (1.0f / mu)) + 1.0f, nia);
+    if (y < y3)
+      return powf((-al / cp) * (lda * y - cm / mu - cm * ((epa - 1.0f) / al)) + epa, nia);
+    return 1.0f - (1.0f / mu) * logf(mu * lda * (1.0f - y) / cp);
+  }
+
+  SDEMC_DI float jump_first(const sdemc_inst& I) {
+    if (I.rate <= 0.f) { jmark = 0.f; jsel = 0; return __int_as_float(0x7f800000); }
+    jblock = 0;
+    return load_jump(I, 0);
+  }
+  SDEMC_DI void jump_mark(int /*k*/, float& J, int& sel) const { J = jmark; sel = jsel; }
+  SDEMC_DI float jump_next(const sdemc_inst& I, float nj) {
+    ++jblock;
+    const float gap = load_jump(I, jblock);
+    return __fadd_rn(nj, gap);
+  }
+  SDEMC_DI int jumps_taken() const { return (int)jblock; }
+};
+
+// Replay draws: increments, marks and jump times recorded from the reference.
+template <int D, int NOISE>
+struct ReplayDraws {
+  using L = Layout<D, NOISE>;
+  const float* dw;      // (S, D * NW) row of this path
+  const float* marks;   // (S)
+  const int32_t* asset; // (S) or null
+  const float* jt;      // (MJ)
+  int S, MJ, jidx;
+  bool overflow;
+
+  SDEMC_DI void increments(const sdemc_inst&, int k, float, float* dW, float* dW2, float*) {
+    if (k >= S) {
+#pragma unroll
+      for (int i = 0; i < D; ++i) { dW[i] = 0.f; dW2[i] = 0.f; }
+      overflow = true;
+      return;
+    }
+    const float* r = dw + (size_t)k * D * L::NW;
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      if (L::NW == 1) { dW[i] = r[i]; dW2[i] = 0.f; }
+      else { dW[i] = r[2 * i]; dW2[i] = r[2 * i + 1]; }
+    }
+  }
+  SDEMC_DI float jump_first(const sdemc_inst& I) {
+    jidx = 0;
+    if (I.rate <= 0.f || MJ <= 0) return __int_as_float(0x7f800000);
+    return jt[0];
+  }
+  SDEMC_DI void jump_mark(int k, float& J, int& sel) const {
+    J = (k < S) ? marks[k] : 0.f;
+    sel = (asset != nullptr && k < S) ? asset[k] : 0;
+  }
+  SDEMC_DI float jump_next(const sdemc_inst&, float) {
+    ++jidx;
+    if (jidx >= MJ) { overflow = true; return __int_as_float(0x7f800000); }
+    return jt[jidx];
+  }
+  SDEMC_DI int jumps_taken() const { return jidx; }
+};
+
+// ------------------------------------------------------------- scheme -----
+// EulerScheme.step (sde_mc/schemes.py:7-10) for the affine coefficient form.
+// EXACT: the reference's unfused float32 order  x + drift*h + diffusion*dW.
+// fast : a fixed chain of fused multiply-adds (mirrored by the oracle).
+template <int D, int NOISE, bool EXACT>
+SDEMC_DI void euler(const sdemc_inst& I, float* x, float dt, const float* dW, const float* dW2) {
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    const float xi = x[i];
+    if (EXACT) {
+      const float dr = __fadd_rn(I.drift_a[i], __fmul_rn(I.drift_b[i], xi));
+      const float sg = __fadd_rn(I.diff_s[i], __fmul_rn(I.diff_q[i], xi));
+      const float base = __fadd_rn(xi, __fmul_rn(dr, dt));
+      if (NOISE == SDEMC_NOISE_DIAG) {
+        x[i] = __fadd_rn(base, __fmul_rn(sg, dW[i]));
+      } else {
+        const float sg2 = __fadd_rn(I.diff2_s[i], __fmul_rn(I.diff2_q[i], xi));
+        x[i] = __fadd_rn(base, __fadd_rn(__fmul_rn(sg, dW[i]), __fmul_rn(sg2, dW2[i])));
+      }
+    } else {
+      const float dr = __fmaf_rn(I.drift_b[i], xi, I.drift_a[i]);
+      const float sg = __fmaf_rn(I.diff_q[i], xi, I.diff_s[i]);
+      float xn = __fmaf_rn(dr, dt, xi);
+      xn = __fmaf_rn(sg, dW[i], xn);
+      if (NOISE != SDEMC_NOISE_DIAG) {
+        const float sg2 = __fmaf_rn(I.diff2_q[i], xi, I.diff2_s[i]);
+        xn = __fmaf_rn(sg2, dW2[i], xn);
+      }
+      x[i] = xn;
+    }
+  }
+}
+
+// add_jumps (sde_mc/solvers.py:140-141, 214-217): x + (g + k*base) * J.
+template <int D, bool EXACT>
+SDEMC_DI void apply_jump(const sdemc_inst& I, float* x, const float* base, float J, int sel) {
+  const bool one = I.jump_target == SDEMC_JUMP_ONE_ASSET;
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    if (one && i != sel) continue;
+    if (EXACT)
+      x[i] = __fadd_rn(x[i], __fmul_rn(__fadd_rn(I.jump_g[i], __fmul_rn(I.jump_k[i], base[i])), J));
+    else
+      x[i] = __fmaf_rn(__fmaf_rn(I.jump_k[i], base[i], I.jump_g[i]), J, x[i]);
+  }
+}
+
+// torch.isclose(next_jump_time, t, atol=1e-12) with the default rtol=1e-5,
+// in float32 as torch evaluates it: |nj - t| <= 1e-12f + |1e-5f * t|.
+SDEMC_DI bool jump_due(float nj, float t) {
+  const float err = fabsf(__fsub_rn(nj, t));
+  const float tol = __fadd_rn(1e-12f, fabsf(__fmul_rn(1e-5f, t)));
+  return (nj == t) || (err <= tol);
+}
+
+// ------------------------------------------------------------- payoff -----
+// Option.__call__ = payoff(transform(x)) (sde_mc/options.py:167-176).
+template <int D>
+SDEMC_DI float payoff(const sdemc_inst& I, const float* xin) {
+  float s[D];
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    const float sp = I.payoff_log ? expf(xin[i]) : xin[i];
+    s[i] = __fmul_rn(I.payoff_scale, sp);
+  }
+  const float K = I.strike;
+  switch (I.payoff) {
+    case SDEMC_PAYOFF_EUROCALL: return s[0] > K ? __fsub_rn(s[0], K) : 0.f;
+    case SDEMC_PAYOFF_EUROPUT: return s[0] < K ? __fsub_rn(K, s[0]) : 0.f;
+    case SDEMC_PAYOFF_BINARY_AON: return s[0] >= K ? s[0] : 0.f;
+    case SDEMC_PAYOFF_DIGITAL: return s[0] > K ? 1.f : 0.f;
+    case SDEMC_PAYOFF_BASKET_ARITH: {
+      float acc = s[0];
+#pragma unroll
+      for (int i = 1; i < D; ++i) acc = __fadd_rn(acc, s[i]);
+      const float m = __fdiv_rn(acc, (float)D);
+      return m > K ? __fsub_rn(m, K) : 0.f;
+    }
+    case SDEMC_PAYOFF_BASKET_GEO: {
+      float acc = logf(s[0]);
+#pragma unroll
+      for (int i = 1; i < D; ++i) acc = __fadd_rn(acc, logf(s[i]));
+      const float m = expf(__fdiv_rn(acc, (float)D));
+      return m > K ? __fsub_rn(m, K) : 0.f;
+    }
+    case SDEMC_PAYOFF_RAINBOW: {
+      float m = s[0];
+#pragma unroll
+      for (int i = 1; i < D; ++i) m = fmaxf(m, s[i]);
+      return m > K ? __fsub_rn(m, K) : 0.f;
+    }
+    case SDEMC_PAYOFF_BESTOF: {
+      float m = s[0];
+#pragma unroll
+      for (int i = 1; i < D; ++i) m = fmaxf(m, s[i]);
+      return fmaxf(m, K);
+    }
+    case SDEMC_PAYOFF_ASIANCALL: {
+      if (D < 2) return 0.f;
+      const float a = __fdiv_rn(s[D > 1 ? 1 : 0], I.T);
+      const float sp = I.payoff_log ? expf(a) : a;
+      return sp > K ? __fsub_rn(sp, K) : 0.f;
+    }
+    case SDEMC_PAYOFF_HESTON_RAINBOW: {
+      float m = s[0];
+#pragma unroll
+      for (int i = 2; i < D; i += 2) m = fmaxf(m, s[i]);
+      return m > K ? __fsub_rn(m, K) : 0.f;
+    }
+    default: return 0.f;
+  }
+}
+
+// ------------------------------------------------------------- sinks ------
+struct NullSink {
+  static constexpr bool kWantsLeft = false;
+  template <int D> SDEMC_DI void init(const float*) {}
+  template <int D, int NW> SDEMC_DI void step(int, const float*, const float*, float, float, int,
+                                              const float*, const float*, const float*, int) {}
+  template <int D, int NW> SDEMC_DI void finish(int, const float*, float) {}
+};
+
+// AdaptedPathData layout (sde_mc/nets.py:192-207 / solvers.py:150-162):
+// paths, left, jumps (S+1, D); time (S+1); normals (S, D*NW); optional raw
+// normals z (S, zdim).  One row per path, S = steps cap.
+struct StoreSink {
+  static constexpr bool kWantsLeft = true;
+  float *paths, *left, *time, *jumps, *normals, *z;
+  int S, zdim;
+
+  template <int D> SDEMC_DI void init(const float* x) {
+    if (paths) for (int i = 0; i < D; ++i) paths[i] = x[i];
+    if (left) for (int i = 0; i < D; ++i) left[i] = x[i];
+    if (jumps) for (int i = 0; i < D; ++i) jumps[i] = 0.f;
+    if (time) time[0] = 0.f;
+  }
+  template <int D, int NW>
+  SDEMC_DI void step(int k, const float* xl, const float* x, float t, float J, int sel,
+                     const float* dW, const float* dW2, const float* zr, int jump_one) {
+    if (k >= S) return;
+    const size_t c = (size_t)(k + 1) * D;
+    if (paths) for (int i = 0; i < D; ++i) paths[c + i] = x[i];
+    if (left) for (int i = 0; i < D; ++i) left[c + i] = xl[i];
+    if (jumps) for (int i = 0; i < D; ++i) jumps[c + i] = (jump_one && i != sel) ? 0.f : J;
+    if (time) time[k + 1] = t;
+    if (normals) {
+      float* n = normals + (size_t)k * D * NW;
+      for (int i = 0; i < D; ++i) {
+        if (NW == 1) n[i] = dW[i];
+        else { n[2 * i] = dW[i]; n[2 * i + 1] = dW2[i]; }
+      }
+    }
+    if (z && zr) for (int j = 0; j < zdim; ++j) z[(size_t)k * zdim + j] = zr[j];
+  }
+  template <int D, int NW>
+  SDEMC_DI void finish(int kend, const float* x, float t) {
+    for (int k = kend; k < S; ++k) {
+      const size_t c = (size_t)(k + 1) * D;
+      if (paths) for (int i = 0; i < D; ++i) paths[c + i] = x[i];
+      if (left) for (int i = 0; i < D; ++i) left[c + i] = x[i];
+      if (jumps) for (int i = 0; i < D; ++i) jumps[c + i] = 0.f;
+      if (time) time[k + 1] = t;
+      if (normals) for (int i = 0; i < D * NW; ++i) normals[(size_t)k * D * NW + i] = 0.f;
+      if (z) for (int j = 0; j < zdim; ++j) z[(size_t)k * zdim + j] = 0.f;
+    }
+  }
+};
+
+// ------------------------------------------------------------ the loop ----
+// One path per lane; the warp steps in lock-step so that step k of every lane
+// draws from block k of its own stream (warp-uniform control, no divergence
+// on refills).  A lane whose t reached T is frozen (dt = 0, no jumps), which
+// is what the reference's batch-global loop does to finished paths
+// (sde_mc/solvers.py:182, 190-191).  Returns the number of active steps.
+template <int D, int NOISE, bool EXACT, class Draws, class Sink>
+SDEMC_DI int simulate(const sdemc_inst& I, Draws& dr, Sink& sk, float* x,
+                      int max_iters, bool& overflow) {
+  using L = Layout<D, NOISE>;
+#pragma unroll
+  for (int i = 0; i < D; ++i) x[i] = I.x0[i];
+  sk.template init<D>(x);
+  float t = 0.f;
+  float dW[D], dW2[D], z[L::ZD];
+#pragma unroll
+  for (int i = 0; i < D; ++i) dW2[i] = 0.f;
+  const int jump_one = I.jump_target == SDEMC_JUMP_ONE_ASSET;
+  int k = 0;
+  if (I.grid == SDEMC_GRID_UNIFORM) {
+    // DiffusionSolver.solve: exactly num_steps steps of h, t += h.
+    const float h = I.h;
+    for (; k < I.num_steps; ++k) {
+      dr.increments(I, k, h, dW, dW2, z);
+      euler<D, NOISE, EXACT>(I, x, h, dW, dW2);
+      t = __fadd_rn(t, h);
+      sk.template step<D, L::NW>(k, x, x, t, 0.f, 0, dW, dW2, z, 0);
+    }
+    sk.template finish<D, L::NW>(k, x, t);
+    return k;
+  }
+  const float T = I.T;
+  float h = I.h;
+  float nj = dr.jump_first(I);
+  int own = 0;
+  bool act = t < T;
+  // mc_simple(payoff_time='terminal') on a jump solver reads column num_steps
+  // of the storage (sde_mc/mc.py:84-86, 92): keep that state when asked.
+  const bool at_nominal = (I.flags & SDEMC_INST_PAYOFF_AT_NOMINAL_STEP) != 0;
+  float xcap[D];
+#pragma unroll
+  for (int i = 0; i < D; ++i) xcap[i] = x[i];
+  while (__any_sync(kFull, act)) {
+    if (k >= max_iters) { overflow = true; break; }
+    // h = min(h, max(T - t, 0)); dt = min(h, next_jump - t)
+    h = fminf(h, fmaxf(__fsub_rn(T, t), 0.f));
+    float dt = fminf(h, __fsub_rn(nj, t));
+    if (!act) dt = 0.f;
+    dr.increments(I, k, dt, dW, dW2, z);
+    float old[D];
+#pragma unroll
+    for (int i = 0; i < D; ++i) old[i] = x[i];
+    euler<D, NOISE, EXACT>(I, x, dt, dW, dW2);
+    t = __fadd_rn(t, dt);
+    float xl[D];
+    if (Sink::kWantsLeft) {
+#pragma unroll
+      for (int i = 0; i < D; ++i) xl[i] = x[i];
+    }
+    float J = 0.f;
+    int sel = 0;
+    if (act && jump_due(nj, t)) {
+      dr.jump_mark(k, J, sel);
+      apply_jump<D, EXACT>(I, x, I.exact_jumps ? x : old, J, sel);
+      nj = dr.jump_next(I, nj);
+    }
+    sk.template step<D, L::NW>(k, Sink::kWantsLeft ? xl : x, x, t, J, sel, dW, dW2, z, jump_one);
+    own += act ? 1 : 0;
+    if (at_nominal && act && own == I.num_steps) {
+#pragma unroll
+      for (int i = 0; i < D; ++i) xcap[i] = x[i];
+    }
+    ++k;
+    act = t < T;
+  }
+  sk.template finish<D, L::NW>(k, x, t);
+  if (at_nominal && own >= I.num_steps) {
+#pragma unroll
+    for (int i = 0; i < D; ++i) x[i] = xcap[i];
+  }
+  return own;
+}
+
+// Warp sum (fixed xor butterfly: every lane ends with the same bits).
+SDEMC_DI float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+
+}  // namespace sdemc

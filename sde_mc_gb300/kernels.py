@@ -1,0 +1,149 @@
+"""Thin typed wrappers over the C ABI: each call takes a lowered instance
+descriptor plus torch CUDA tensors and launches on the current stream.
+
+These are the only entry points the estimator modules use; they are also
+registered as torch ops (``torch.ops.sdemc.*``) in :mod:`sde_mc_gb300.torch_ops`.
+"""
+import ctypes
+
+import torch
+
+from . import _native as N
+
+
+def _dev(device):
+    return N.require_cuda(device)
+
+
+def price(inst, cfg=None, payoffs=None, device=None, out=None):
+    """Fused K1 launch.  Returns a float64 CUDA tensor
+    (sum, sum_sq, n, mean, var, status) without synchronising."""
+    dev = _dev(device)
+    lib = N.load()
+    need = lib.sdemc_price_scratch_bytes(ctypes.byref(inst))
+    scratch = N.SCRATCH.get(need, dev)
+    if out is None:
+        out = torch.empty(6, dtype=torch.float64, device=dev)
+    if payoffs is not None:
+        assert payoffs.is_cuda and payoffs.dtype == torch.float32 and payoffs.numel() >= inst.num_paths
+    rc = lib.sdemc_price(ctypes.byref(inst), N.byref(cfg), N.ptr(scratch), scratch.numel(), N.ptr(out),
+                         N.ptr(payoffs), N.stream_handle(dev))
+    N.check(rc, "sdemc_price")
+    return out
+
+
+def mlmc_level(inst, fine, coarse, h_fine, h_coarse, cfg=None, ys=None, device=None, out=None):
+    """K2 launch for one level.  Returns float64 CUDA tensor
+    (sumY, sumY2, n, sumPf, sumPf2, mean, var, status)."""
+    dev = _dev(device)
+    lib = N.load()
+    need = lib.sdemc_mlmc_scratch_bytes(ctypes.byref(inst))
+    scratch = N.SCRATCH.get(need, dev)
+    if out is None:
+        out = torch.empty(8, dtype=torch.float64, device=dev)
+    rc = lib.sdemc_mlmc_level(ctypes.byref(inst), int(fine), int(coarse), float(h_fine), float(h_coarse),
+                              N.byref(cfg), N.ptr(scratch), scratch.numel(), N.ptr(out), N.ptr(ys),
+                              N.stream_handle(dev))
+    N.check(rc, "sdemc_mlmc_level")
+    return out
+
+
+def zdim(dim, noise):
+    return dim if noise == N.NOISE_DIAG else (dim + 1 if noise == N.NOISE_INDEP_SHARED else 2 * dim)
+
+
+def materialise(inst, steps_cap, want=("paths", "left", "time", "jumps", "normals", "payoffs", "steps"),
+                export_draws=False, jcap=0, device=None):
+    """K4: full storage of num_paths paths at steps_cap columns.  Returns a dict
+    of CUDA tensors (plus 'status').  export_draws adds raw normals 'z' and the
+    jump stream 'jt', 'jm', 'jsel' (jcap entries per path) for the oracle."""
+    dev = _dev(device)
+    n, d, S = int(inst.num_paths), int(inst.dim), int(steps_cap)
+    nw = 1 if inst.noise == N.NOISE_DIAG else 2
+    f32 = dict(dtype=torch.float32, device=dev)
+    out = {}
+    if "paths" in want:
+        out["paths"] = torch.empty((n, S + 1, d), **f32)
+    if "left" in want:
+        out["left"] = torch.empty((n, S + 1, d), **f32)
+    if "time" in want:
+        out["time"] = torch.empty((n, S + 1), **f32)
+    if "jumps" in want:
+        out["jumps"] = torch.empty((n, S + 1, d), **f32)
+    if "normals" in want:
+        out["normals"] = torch.empty((n, S, d) if nw == 1 else (n, S, d, 2), **f32)
+    if "payoffs" in want:
+        out["payoffs"] = torch.empty(n, **f32)
+    if "steps" in want:
+        out["steps"] = torch.empty(n, dtype=torch.int32, device=dev)
+    zd = zdim(d, inst.noise)
+    if export_draws:
+        out["z"] = torch.empty((n, S, zd), **f32)
+        if jcap > 0:
+            out["jt"] = torch.empty((n, jcap), **f32)
+            out["jm"] = torch.empty((n, jcap), **f32)
+            out["jsel"] = torch.empty((n, jcap), dtype=torch.int32, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    g = out.get
+    rc = N.load().sdemc_materialise(
+        ctypes.byref(inst), S, N.ptr(g("paths")), N.ptr(g("left")), N.ptr(g("time")), N.ptr(g("jumps")),
+        N.ptr(g("normals")), N.ptr(g("payoffs")), N.ptr(g("steps")), N.ptr(g("z")), zd, N.ptr(g("jt")),
+        N.ptr(g("jm")), N.ptr(g("jsel")), int(jcap) if export_draws else 0, N.ptr(status),
+        N.stream_handle(dev))
+    N.check(rc, "sdemc_materialise")
+    out["status"] = status
+    return out
+
+
+def replay(inst, dw, jump_times=None, marks=None, asset=None, device=None):
+    """K3: replay recorded draws.  dw (bs, S, d[, 2]); jump_times (bs, MJ);
+    marks/asset (bs, S).  Returns dict of paths/left/time/jumps/payoffs/steps/status."""
+    dev = _dev(device)
+    bs, S = int(dw.shape[0]), int(dw.shape[1])
+    d = int(inst.dim)
+    f32 = dict(dtype=torch.float32, device=dev)
+
+    def c(t, dt=torch.float32):
+        return None if t is None else t.to(device=dev, dtype=dt).contiguous()
+    dw, jump_times, marks, asset = c(dw), c(jump_times), c(marks), c(asset, torch.int32)
+    out = dict(paths=torch.empty((bs, S + 1, d), **f32), left=torch.empty((bs, S + 1, d), **f32),
+               time=torch.empty((bs, S + 1), **f32), jumps=torch.empty((bs, S + 1, d), **f32),
+               payoffs=torch.empty(bs, **f32), steps=torch.empty(bs, dtype=torch.int32, device=dev),
+               status=torch.zeros(1, dtype=torch.int32, device=dev))
+    mj = int(jump_times.shape[1]) if jump_times is not None else 0
+    rc = N.load().sdemc_replay(ctypes.byref(inst), bs, S, mj, N.ptr(jump_times), N.ptr(dw), N.ptr(marks),
+                               N.ptr(asset), N.ptr(out["paths"]), N.ptr(out["left"]), N.ptr(out["time"]),
+                               N.ptr(out["jumps"]), N.ptr(out["payoffs"]), N.ptr(out["steps"]),
+                               N.ptr(out["status"]), N.stream_handle(dev))
+    N.check(rc, "sdemc_replay")
+    return out
+
+
+def mlmc_replay(inst, fine, coarse, h_fine, h_coarse, dw, coarse_cap, jump_times=None, marks=None,
+                asset=None, device=None):
+    dev = _dev(device)
+    bs, Sf = int(dw.shape[0]), int(dw.shape[1])
+    d = int(inst.dim)
+
+    def c(t, dt=torch.float32):
+        return None if t is None else t.to(device=dev, dtype=dt).contiguous()
+    dw, jump_times, marks, asset = c(dw), c(jump_times), c(marks), c(asset, torch.int32)
+    xf = torch.empty((bs, d), dtype=torch.float32, device=dev)
+    xc = torch.empty((bs, d), dtype=torch.float32, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    mj = int(jump_times.shape[1]) if jump_times is not None else 0
+    rc = N.load().sdemc_mlmc_replay(ctypes.byref(inst), int(fine), int(coarse), float(h_fine),
+                                    float(h_coarse), bs, Sf, int(coarse_cap), mj, N.ptr(jump_times),
+                                    N.ptr(dw), N.ptr(marks), N.ptr(asset), N.ptr(xf), N.ptr(xc),
+                                    N.ptr(status), N.stream_handle(dev))
+    N.check(rc, "sdemc_mlmc_replay")
+    return dict(xf=xf, xc=xc, status=status)
+
+
+def philox(seed, stream_id, tag, path, first_block, nblocks, device=None):
+    dev = _dev(device)
+    out = torch.empty((nblocks, 4), dtype=torch.int32, device=dev)
+    rc = N.load().sdemc_philox(int(seed), int(stream_id), int(tag), int(path), int(first_block),
+                               int(nblocks), N.ptr(out), N.stream_handle(dev))
+    N.check(rc, "sdemc_philox")
+    return out

@@ -1,0 +1,167 @@
+"""CPU-side checks: the C-ABI library loads and exports every declared symbol,
+the ctypes descriptor matches the C layout, and the host-side API (lowering,
+payoffs, helpers, closed forms) matches the reference's known answers."""
+import os
+import re
+
+import numpy as np
+import pytest
+import torch
+
+import sde_mc_gb300 as sm
+from sde_mc_gb300 import _native as N
+from sde_mc_gb300.lowering import lower, max_jumps_for
+from tests.cases import FIXTURE_CASES, inst_for, indep2d, merton1d
+from tests.conftest import ROOT, load_npz
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "sdemc.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:int|size_t)\s+(sdemc_\w+)\s*\(", src, flags=re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = N.load()
+    decl = declared_symbols()
+    assert len(decl) >= 14
+    for name in decl:
+        assert hasattr(lib, name), name
+    assert set(decl) == set(N.EXPORTED)
+
+
+def test_descriptor_layout_matches_header():
+    lib = N.load()
+    assert lib.sdemc_abi_version() == 1
+    assert lib.sdemc_inst_size() == __import__("ctypes").sizeof(N.SdemcInst)
+    assert N.abi_offsets() == N.ctypes_offsets()
+
+
+def test_scratch_sizes():
+    import ctypes
+    inst = inst_for(merton1d(), num_paths=1000)
+    lib = N.load()
+    nch = (1000 + 127) // 128
+    assert lib.sdemc_price_scratch_bytes(ctypes.byref(inst)) == 256 + nch * 3 * 8
+    assert lib.sdemc_mlmc_scratch_bytes(ctypes.byref(inst)) == 256 + nch * 5 * 8
+
+
+def test_lowering_uses_reference_float32_coefficients(kat):
+    inst = inst_for(merton1d(), num_paths=10)
+    assert inst.drift_b[0] == np.float32(kat["merton_c1_drift_coef"])
+    assert inst.diff_q[0] == np.float32(0.2)
+    assert inst.h == np.float32(1.0 / 100)
+    assert inst.rate == 2.0 and inst.mark == N.MARK_LOGNORMAL
+    for name, factory in FIXTURE_CASES.items():
+        fx = load_npz(name)
+        ins = inst_for(factory(), num_paths=4)
+        if "coef_b" in fx:
+            np.testing.assert_array_equal(np.array(ins.drift_b[:ins.dim], np.float32), fx["coef_b"].reshape(-1))
+        L = fx["chol"]
+        packed = [L[i, j] for i in range(ins.dim) for j in range(i + 1)]
+        np.testing.assert_array_equal(np.array(ins.chol[:len(packed)], np.float32), np.array(packed, np.float32))
+
+
+def test_max_jumps_matches_reference(kat):
+    for key, v in kat["max_jumps"].items():
+        lam, T = map(float, key.split("_"))
+        assert max_jumps_for(lam, T) == v
+        m = sm.Merton(0.02, 0.2, lam, -0.1, 0.2, torch.tensor([1.]), dim=1)
+        assert sm.JumpEulerSolver(m, T, 10).max_jumps == v
+
+
+def test_payoffs_match_reference(kat):
+    make = {"EuroCall": lambda: sm.EuroCall(1), "EuroPut": lambda: sm.EuroPut(1),
+            "BinaryAoN": lambda: sm.BinaryAoN(1), "Digital": lambda: sm.Digital(1.), "Basket": lambda: sm.Basket(1),
+            "BasketGeo": lambda: sm.Basket(0.8, 'geometric'), "Rainbow": lambda: sm.Rainbow(1),
+            "BestOf": lambda: sm.BestOf(1), "HestonRainbow": lambda: sm.HestonRainbow(1.0),
+            "AsianCall": lambda: sm.AsianCall(2.0, 0.5),
+            "EuroCallLog": lambda: sm.EuroCall(1.0, log=True, discount=0.9),
+            "RainbowLog": lambda: sm.Rainbow(1.0, log=True, discount=1.05), "Basket4": lambda: sm.Basket(1.0)}
+    for name, case in kat["payoffs"].items():
+        got = make[name]()(torch.tensor(case["x"]))
+        np.testing.assert_allclose(got.numpy(), np.array(case["out"]), rtol=1e-6, atol=1e-7, err_msg=name)
+
+
+def test_helpers_match_reference(kat):
+    for e, v in kat["partition"].items():
+        np.testing.assert_allclose(sm.partition(3, 3, e).numpy(), v)
+    q = kat["solve_quadratic"]
+    got = sm.solve_quadratic((torch.tensor(q["a"]), torch.tensor(q["b"]), torch.tensor(q["c"])))
+    np.testing.assert_allclose(got.numpy(), q["out"], rtol=1e-6)
+    s = torch.tensor(kat["mc_estimates"]["sample"])
+    m, v = sm.mc_estimates(s.sum(), (s * s).sum(), len(s))
+    assert float(m) == pytest.approx(kat["mc_estimates"]["mean"], rel=1e-6)
+    assert float(v) == pytest.approx(kat["mc_estimates"]["var"], rel=1e-6)
+    np.testing.assert_allclose(sm.get_corr_matrix(kat["get_corr_matrix"]["rhos"]).numpy(),
+                               kat["get_corr_matrix"]["out"], rtol=1e-6)
+    args, v = kat["remove_steps"]
+    assert sm.remove_steps(*args) == v
+    args, v = kat["ceil_mult"]
+    assert sm.ceil_mult(*args) == v
+    with pytest.raises(AssertionError):
+        sm.get_corr_matrix([0.1, 0.2])
+    with pytest.raises(RuntimeError):
+        sm.get_corr_matrix([0.99, 0.99, -0.99])
+
+
+def test_closed_forms_match_reference(kat):
+    for args, v in kat["merton_call"]:
+        assert sm.merton_call(*args) == pytest.approx(v, rel=1e-12)
+    assert sm.bs_call(*kat["bs_call"][0]) == pytest.approx(kat["bs_call"][1], rel=1e-12)
+    assert sm.bs_binary_aon(*kat["bs_binary_aon"][0]) == pytest.approx(kat["bs_binary_aon"][1], rel=1e-9)
+    assert sm.bs_digital_call(*kat["bs_digital_call"][0]) == pytest.approx(kat["bs_digital_call"][1], rel=1e-10)
+    assert sm.bs_asian_call(*kat["bs_asian_call"][0]) == pytest.approx(kat["bs_asian_call"][1], rel=1e-12)
+    c = kat["constant_short_rate"]
+    np.testing.assert_allclose(sm.ConstantShortRate(c["r"])(torch.tensor(c["t"])).numpy(), c["out"])
+    assert float(sm.ConstantShortRate(c["r"])(1.0)) == pytest.approx(c["scalar"])
+
+
+def test_levy_objects_match_reference(kat):
+    ic = kat["inverse_cdf"]
+    icdf = sm.InverseCdf(*ic["params"][:2], ic["params"][2], ic["params"][3], ic["params"][4])
+    assert icdf.lda == pytest.approx(ic["lda"]) and icdf.y2 == pytest.approx(ic["y2"])
+    np.testing.assert_allclose(icdf(torch.tensor(ic["y"])).numpy(), ic["out"], rtol=1e-5, atol=1e-6)
+    assert sm.get_jump_comp(*kat["get_jump_comp"][0]) == pytest.approx(kat["get_jump_comp"][1], rel=1e-9)
+    ev = sm.ExpExampleLevy(1, 1, 0.5, 2, 0.02, 0.2, 0.1, 0.01)
+    assert ev.gamma() == pytest.approx(kat["exp_example_levy"]["gamma"])
+    assert ev.beta() == pytest.approx(kat["exp_example_levy"]["beta"])
+
+
+def test_sde_interfaces():
+    g = sm.Gbm(0.02, 0.2, torch.tensor([1., 2.]), dim=2)
+    assert g.diffusion_struct == 'diag' and g.brown_dim == 2 and g.jump_rate() == 0
+    x0 = g.init_value
+    assert torch.allclose(g.drift(0, x0), 0.02 * x0)
+    m = sm.Merton(0.02, 0.3, 2, -0.05, 0.3, torch.tensor([1., 1.]), dim=2)
+    assert torch.allclose(m.drift(0, x0), (0.02 - m.jump_mean() * 2) * x0)
+    assert m.sample_jumps((3, 4, 2), 'cpu').shape == (3, 4, 2)
+    h = sm.Heston(0.02, 0.5, 0.1, 0.15, -0.5, torch.tensor([1., 2.]))
+    assert torch.allclose(h.corr_matrix, torch.tensor([[1, -0.5], [-0.5, 1]]))
+    ind = indep2d()[0].sde
+    assert torch.allclose(ind.jump_rate(), torch.tensor([1., 1.]))
+    assert ind.sample_jumps((5, 1), 'cpu').shape == (5, 2)
+
+
+def test_unknown_model_is_not_lowered():
+    class Custom(sm.DiffusionSde):
+        def drift(self, t, x):
+            return x * x
+
+        def diffusion(self, t, x):
+            return x
+
+    s = sm.EulerSolver(Custom(torch.ones(1), 1, 1, 'diag'), 1.0, 10)
+    with pytest.raises(NotImplementedError):
+        lower(s, sm.EuroCall(1.0), None, num_paths=10)
+    with pytest.raises(NotImplementedError):
+        lower(sm.JumpEulerSolver(sm.Gbm(0.1, 0.2, torch.ones(9), 9), 1.0, 10), sm.Basket(1.0), None, 10)
+
+
+@pytest.mark.skipif(torch.cuda.is_available(), reason="checks the no-GPU behaviour")
+def test_no_cpu_fallback():
+    solver, payoff, disc = merton1d()
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        sm.mc_simple(1000, solver, payoff, disc, bs=1000)
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        solver.solve(8)

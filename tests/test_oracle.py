@@ -1,0 +1,161 @@
+"""The oracle pinned against the reference: known-answer values and the draws
+and outputs recorded from the reference's own solver runs (tests/golden)."""
+import math
+
+import numpy as np
+import pytest
+
+from tests.cases import FIXTURE_CASES, inst_for, merton1d, indep2d
+from tests.conftest import load_npz
+
+
+def test_philox_known_answers(oracle_mod):
+    # Random123's published Philox4x32-10 known-answer vectors (Salmon et al., SC'11)
+    import ctypes
+    lib = oracle_mod.load()
+    # counter = (block, c1, c2, c3): reproduce through the seed/stream/path mapping
+    # ctr (0,0,0,0) key (0,0)
+    out = oracle_mod.philox(0, 0, 0, 0, 0, 1)[0]
+    assert [int(v) for v in out] == [0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8]
+    # ctr all ones, key all ones: block=0xffffffff, path lo=0xffffffff,
+    # c2 = path_hi(0xffff) | tag 0xffff << 16, stream=0xffffffff
+    out = oracle_mod.philox(0xFFFFFFFFFFFFFFFF, 0xFFFFFFFF, 0xFFFF, 0x0000FFFFFFFFFFFF, 0xFFFFFFFF, 1)[0]
+    assert [int(v) for v in out] == [0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd]
+    out = oracle_mod.philox(0x299f31d0a4093822, 0x03707344, 0x1319, 0x8a2e85a308d3, 0x243f6a88, 1)[0]
+    assert [int(v) for v in out] == [0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1]
+
+
+def test_closed_forms(oracle_mod, kat):
+    args, v = kat["bs_call"]
+    assert oracle_mod.bs_call(*args) == pytest.approx(v, rel=1e-12)
+    args, v = kat["bs_binary_aon"]
+    assert oracle_mod.bs_binary_aon(*args) == pytest.approx(v, rel=1e-9)
+    for args, v in kat["merton_call"]:
+        assert oracle_mod.merton_call(*args) == pytest.approx(v, rel=1e-12)
+    args, v = kat["bs_digital_call"]
+    assert oracle_mod.bs_digital_call(*args) == pytest.approx(v, rel=1e-10)
+    args, v = kat["bs_asian_call"]
+    assert oracle_mod.bs_asian_call(*args) == pytest.approx(v, rel=1e-12)
+    assert oracle_mod.merton_call(1, 1, 3, 0.02, 0.3, -0.05, 0.3, 2) == pytest.approx(0.36328189504657027, rel=1e-12)
+
+
+def test_mc_estimates(oracle_mod, kat):
+    s = np.array(kat["mc_estimates"]["sample"], np.float64)
+    m, v = oracle_mod.mc_estimates(s.sum(), (s * s).sum(), len(s))
+    assert m == pytest.approx(kat["mc_estimates"]["mean"], rel=1e-6)
+    assert v == pytest.approx(kat["mc_estimates"]["var"], rel=1e-6)
+
+
+def _replay(oracle_mod, name):
+    fx = load_npz(name)
+    inst = inst_for(FIXTURE_CASES[name](), num_paths=int(fx["bs"]))
+    if inst.grid == 1:
+        out = oracle_mod.replay(inst, fx["dw"])
+    else:
+        out = oracle_mod.replay(inst, fx["dw"], fx["jump_times"], fx["marks"], fx.get("asset"))
+    return fx, inst, out
+
+
+@pytest.mark.parametrize("name", ["replay_merton1d", "replay_merton2d_corr", "replay_merton2d_exact",
+                                  "replay_indep2d", "replay_gbm_uniform"])
+def test_replay_bit_exact_vs_reference(oracle_mod, name):
+    """Recorded reference draws through the oracle's loop give the reference's
+    paths, time grid, left limits, jump marks and payoffs bit for bit."""
+    fx, inst, out = _replay(oracle_mod, name)
+    assert out["rc"] == 0
+    S = fx["paths"].shape[1] - 1
+    np.testing.assert_array_equal(out["paths"][:, :S + 1], fx["paths"])
+    if "time" in fx:
+        np.testing.assert_array_equal(out["time"], fx["time"])
+        np.testing.assert_array_equal(out["left"], fx["left"])
+        np.testing.assert_array_equal(out["jumps"], expected_jump_paths(fx))
+        assert int(out["steps"].max()) == int(fx["S"])
+        np.testing.assert_array_equal(out["payoffs"], fx["payoffs"])
+
+
+def expected_jump_paths(fx):
+    """The per-asset adapter stores its encoded mark 10k + (1 + Y) in every
+    column; the kernels store Y in asset k's column only.  Decode with the
+    adapter's own float32 operations."""
+    if "asset" not in fx:
+        return fx["jumps"]
+    m = fx["jumps"][..., 0].astype(np.float32)
+    k = np.floor(m / np.float32(10.0))
+    y = (m - np.float32(10.0) * k - np.float32(1.0)).astype(np.float32)
+    out = np.zeros_like(fx["jumps"])
+    for i in range(out.shape[-1]):
+        out[..., i] = np.where((m != 0) & (k == i), y, np.float32(0.0))
+    return out
+
+
+def test_replay_levy_within_tolerance(oracle_mod):
+    """The Levy drift folds -f*gamma into one coefficient, so it is 1e-5-close,
+    not bit-exact; the time grid (pure float adds/mins) is still exact."""
+    fx, inst, out = _replay(oracle_mod, "replay_levy2d")
+    assert out["rc"] == 0
+    np.testing.assert_array_equal(out["time"], fx["time"])
+    np.testing.assert_allclose(out["paths"], fx["paths"], rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(out["payoffs"], fx["payoffs"], rtol=1e-5, atol=1e-6)
+
+
+@pytest.mark.parametrize("name,factory,levels", [("mlmc_merton1d", lambda: merton1d(4), (8, 4)),
+                                                 ("mlmc_indep2d", lambda: indep2d(8), (16, 8))])
+def test_mlmc_replay_bit_exact(oracle_mod, name, factory, levels):
+    fx = load_npz(name)
+    inst = inst_for(factory(), num_paths=int(fx["bs"]), steps=levels[1])
+    out = oracle_mod.mlmc_replay(inst, levels[0] // levels[1], float(fx["h_fine"]), float(fx["h_coarse"]),
+                                 fx["dw"], fx["marks"].shape[1], fx["jump_times"], fx["marks"], fx.get("asset"))
+    assert out["rc"] == 0
+    np.testing.assert_array_equal(out["xf"], fx["xf"])
+    np.testing.assert_array_equal(out["xc"], fx["xc"])
+
+
+def test_cv_mlp_grads_and_adam(oracle_mod):
+    """Hand-written backprop of Var(payoff + sum e^{-rt} f . dW) and one Adam
+    step agree with torch autograd + torch.optim.Adam run by the reference."""
+    fx = load_npz("cv_mlp")
+    params = [fx["p0_%d" % i].astype(np.float64) for i in range(8)]
+    loss, gamma, grads = oracle_mod.cv_loss_and_grads(params, fx["f_in"].astype(np.float64),
+                                                      fx["normals"].astype(np.float64),
+                                                      fx["time"][..., 0].astype(np.float64),
+                                                      fx["payoffs"].astype(np.float64), float(fx["r"]))
+    assert loss == pytest.approx(float(fx["loss"]), rel=1e-4)
+    np.testing.assert_allclose(gamma, fx["gamma"], rtol=1e-4, atol=1e-6)
+    for i in range(8):
+        np.testing.assert_allclose(grads[i], fx["grad_%d" % i], rtol=2e-3, atol=1e-7)
+    new, _ = oracle_mod.adam_step(params, grads, lr=1e-3)
+    for i in range(8):
+        np.testing.assert_allclose(new[i], fx["p1_%d" % i], rtol=1e-5, atol=1e-6)
+
+
+def test_native_price_vs_merton_closed_form(oracle_mod, kat, ref_stats):
+    """The oracle's own Philox draws through the reference loop price config 1
+    within 3 standard errors of the Merton series and of the reference's run."""
+    case = merton1d(100)
+    inst = inst_for(case, num_paths=1 << 17, seed=11)
+    out, _, rc = oracle_mod.price(inst)
+    assert rc == 0
+    mean, var = out[3], out[4]
+    se = math.sqrt(var / out[2])
+    exact = kat["merton_call"][1][1]
+    assert abs(mean - exact) < 3 * se + 1e-4  # Euler bias at 100 steps is below 1e-4
+    r = ref_stats["c1_fp32_2p18"]
+    assert abs(mean - r["mean"]) < 3 * math.hypot(se, r["se"])
+
+
+def test_native_price_c2_vs_reference(oracle_mod, ref_stats):
+    inst = inst_for(indep2d(256), num_paths=1 << 15, seed=5)
+    out, _, rc = oracle_mod.price(inst)
+    assert rc == 0
+    se = math.sqrt(out[4] / out[2])
+    r = ref_stats["c2_plain_2p16"]
+    assert abs(out[3] - r["mean"]) < 3 * math.hypot(se, r["se"])
+
+
+def test_chunk_reduce_matches_fp64_sum(oracle_mod):
+    rng = np.random.default_rng(0)
+    v = rng.random(1000).astype(np.float32)
+    out = oracle_mod.chunk_reduce(v)
+    assert out[2] == 1000
+    assert out[0] == pytest.approx(float(v.astype(np.float64).sum()), rel=1e-6)
+    assert out[3] == pytest.approx(float(v.mean()), rel=1e-6)
