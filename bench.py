@@ -41,12 +41,26 @@ WORKLOAD = ("config-2 2D rainbow (call on max), Merton assets with independent p
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--rel", type=float, default=1e-3)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--profile-paths", type=int, default=0,
+                    help="profiling driver: make three price launches of the workload at this many paths "
+                         "and exit (the case ncu captures)")
     return ap.parse_args()
+
+
+def profile_launches(n):
+    import torch
+    from sde_mc_gb300 import kernels as K
+    from sde_mc_gb300.lowering import lower
+    solver, payoff, disc = make_problem()
+    for i in range(3):
+        r = K.price(lower(solver, payoff, disc, num_paths=n, path_offset=i * n, seed=1))
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_paths": n, "result": r.cpu().tolist()}))
 
 
 def dist_env():
@@ -194,6 +208,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_paths:
+        return profile_launches(args.profile_paths)
     import torch
     import torch.distributed as dist
     rank, world, local = dist_env()

@@ -90,8 +90,8 @@ extern "C" int sdemc_price_chunks(const sdemc_inst* h_inst, const sdemc_cfg* h_c
   if (scratch_bytes < sdemc_price_scratch_bytes(h_inst))
     return fail(SDEMC_ENOMEM, "scratch %zu bytes < required %zu", scratch_bytes,
                 sdemc_price_scratch_bytes(h_inst));
-  if (h_cfg && h_cfg->block_threads % 32 != 0)
-    return fail(SDEMC_EINVAL, "block_threads %d not a multiple of 32", h_cfg->block_threads);
+  if (h_cfg && (h_cfg->block_threads % 32 != 0 || h_cfg->block_threads > 256 || h_cfg->block_threads < 0))
+    return fail(SDEMC_EINVAL, "block_threads %d: need a multiple of 32 in [32, 256]", h_cfg->block_threads);
   sdemc_cfg cfg{};
   if (h_cfg) cfg = *h_cfg;
   const sdemc_inst& I = *h_inst;

@@ -129,10 +129,10 @@ def test_native_draws_match_oracle_transforms(name, oracle_mod):
     z = np_(out["z"])
     steps = np_(out["steps"])
     for p in range(0, 64, 9):
-        zo = oracle_mod.native_normals(inst, 12345 + p, int(steps[p]), zdim(inst))
+        zo = oracle_mod.native_normals(inst, p, int(steps[p]), zdim(inst))
         np.testing.assert_allclose(z[p, :steps[p]], zo, rtol=2e-5, atol=2e-5)
         if jcap:
-            jt, jm, js = oracle_mod.native_jumps(inst, 12345 + p, jcap)
+            jt, jm, js = oracle_mod.native_jumps(inst, p, jcap)
             np.testing.assert_allclose(np_(out["jt"])[p], jt, rtol=2e-6)
             np.testing.assert_allclose(np_(out["jm"])[p], jm, rtol=2e-5, atol=2e-6)
             np.testing.assert_array_equal(np_(out["jsel"])[p], js)
@@ -157,7 +157,7 @@ def test_fused_price_matches_materialised_and_reduction(name, oracle_mod):
 def test_price_invariant_to_launch_shape():
     inst = inst_for(indep2d(64), num_paths=100_000, seed=3)
     base = np_(K.price(inst))
-    for bt, cps in [(32, 1), (64, 3), (256, 2), (128, 0), (512, 1)]:
+    for bt, cps in [(32, 1), (64, 3), (256, 2), (128, 0), (96, 5)]:
         cfg = N.SdemcCfg(block_threads=bt, ctas_per_sm=cps)
         np.testing.assert_array_equal(np_(K.price(inst, cfg=cfg)), base)
 
