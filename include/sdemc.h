@@ -189,6 +189,25 @@ int sdemc_price_chunks(const sdemc_inst* h_inst, const sdemc_cfg* h_cfg,
 int sdemc_reduce_chunks(void* d_scratch, int64_t nchunks, int width,
                         double* d_out, void* stream);
 
+/* ---- pricing without allocation ----------------------------------------
+ * No counterpart in the reference (which has no native code): sdemc_price for
+ * callers that cannot allocate device memory — a host that owns all GPU
+ * memory through its own pool, or code that must not call cudaMalloc while
+ * it builds a CUDA graph.  The caller passes only d_out (6 doubles, as
+ * sdemc_price) and the optional d_payoffs; the scratch is a fixed array of
+ * sdemc_price_noalloc_scratch_bytes() (~1.5 MB) inside the library, held on
+ * every GPU that loads the library until the process exits.  Calls with more
+ * than SDEMC_NOALLOC_MAX_PATHS paths fail with SDEMC_ENOMEM.  The first call
+ * on each device looks up the array's device address (cudaGetSymbolAddress)
+ * with that device current, so make that first call before any stream
+ * capture.  All calls share the one array: calls that overlap on the GPU
+ * (different streams, or different host threads, on one device) race and
+ * must be serialised by the caller.  Nothing here calls cudaMalloc/cudaFree. */
+#define SDEMC_NOALLOC_MAX_PATHS (1 << 23)
+size_t sdemc_price_noalloc_scratch_bytes(void);
+int sdemc_price_noalloc(const sdemc_inst* h_inst, const sdemc_cfg* h_cfg,
+                        double* d_out, float* d_payoffs, void* stream);
+
 /* ---- K3: replay of recorded draws --------------------------------------
  * Runs the reference's jump-adapted loop (sde_mc/solvers.py:164-226, or its
  * uniform-grid twin :68-88) on draws exported from the reference: d_jump_times

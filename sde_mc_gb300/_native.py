@@ -76,6 +76,8 @@ _PROTOS = {
     "sdemc_price": (_I, [_P, _P, _P, ctypes.c_size_t, _P, _P, _P]),
     "sdemc_price_chunks": (_I, [_P, _P, _P, ctypes.c_size_t, _P, _P]),
     "sdemc_reduce_chunks": (_I, [_P, ctypes.c_int64, _I, _P, _P]),
+    "sdemc_price_noalloc_scratch_bytes": (ctypes.c_size_t, []),
+    "sdemc_price_noalloc": (_I, [_P, _P, _P, _P, _P]),
     "sdemc_replay": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "sdemc_materialise": (_I, [_P, _I, _P, _P, _P, _P, _P, _P, _P, _P, _I, _P, _P, _P, _I, _P, _P]),
     "sdemc_mlmc_scratch_bytes": (ctypes.c_size_t, [_P]),

@@ -8,6 +8,8 @@
 // A chunk of SDEMC_CHUNK_PATHS consecutive paths (32 lanes x 4 rounds) is
 // reduced by a fixed warp butterfly and stored as (sum, sum_sq, n) in FP64 at
 // its own slot, so the bits never depend on the grid shape.
+#include <mutex>
+
 #include "sdemc_device.cuh"
 #include "sdemc_host.cuh"
 
@@ -123,4 +125,66 @@ extern "C" int sdemc_price(const sdemc_inst* h_inst, const sdemc_cfg* h_cfg, voi
   int rc = sdemc_price_chunks(h_inst, h_cfg, d_scratch, scratch_bytes, d_payoffs, stream);
   if (rc) return rc;
   return sdemc_reduce_chunks(d_scratch, num_chunks(h_inst), 3, d_out, stream);
+}
+
+// ---------------------------------------------------------------------------
+// Pricing without any allocation, for callers that cannot call cudaMalloc.
+//
+// Some hosts of this library own the GPU's memory themselves: a process that
+// hands out all device memory through its own pool (so a stray cudaMalloc
+// would fail or fragment it), code running inside a CUDA graph it is building,
+// or a plugin whose host forbids allocations from third-party code.  Those
+// callers still pass their inputs and outputs, but cannot provide scratch.
+// sdemc_price_noalloc keeps the per-chunk partials and the status word in the
+// array below, which lives in this library's module: every GPU that loads the
+// library holds kNoallocScratchBytes (about 1.5 MB) of it until the process
+// exits.  The limit is SDEMC_NOALLOC_MAX_PATHS paths per call.
+// ---------------------------------------------------------------------------
+static constexpr int64_t kNoallocMaxChunks =
+    ((int64_t)SDEMC_NOALLOC_MAX_PATHS + kChunk - 1) / kChunk;
+static constexpr size_t kNoallocScratchBytes = kScratchHeader + (size_t)kNoallocMaxChunks * 3 * sizeof(double);
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
+
+// Device address of g_noalloc_scratch, looked up once per device.  In host code
+// the symbol is only a host-side stand-in, so the address must come from
+// cudaGetSymbolAddress with that device current.
+static constexpr int kNoallocMaxDevices = 64;
+static void* g_noalloc_addr[kNoallocMaxDevices] = {};
+static std::mutex g_noalloc_mutex;
+
+static int noalloc_scratch_address(void** out) {
+  int dev = 0;
+  int rc = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+  if (rc) return rc;
+  if (dev < 0 || dev >= kNoallocMaxDevices) return fail(SDEMC_EINVAL, "device %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    rc = check_cuda(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(no-alloc scratch)");
+    if (rc) return rc;
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return SDEMC_OK;
+}
+
+extern "C" size_t sdemc_price_noalloc_scratch_bytes(void) { return kNoallocScratchBytes; }
+
+extern "C" int sdemc_price_noalloc(const sdemc_inst* h_inst, const sdemc_cfg* h_cfg, double* d_out,
+                                   float* d_payoffs, void* stream) {
+  int rc = validate_inst(h_inst);
+  if (rc) return rc;
+  if (!d_out) return fail(SDEMC_EINVAL, "null output");
+  if (h_inst->num_paths > (int64_t)SDEMC_NOALLOC_MAX_PATHS)
+    return fail(SDEMC_ENOMEM, "num_paths %lld exceeds the no-allocation limit of %d paths per call",
+                (long long)h_inst->num_paths, SDEMC_NOALLOC_MAX_PATHS);
+  void* scratch = nullptr;
+  if ((rc = noalloc_scratch_address(&scratch))) return rc;
+  // The array keeps the previous call's contents: the status word must start
+  // at zero (the chunk partials are all rewritten by this call).
+  if ((rc = check_cuda(cudaMemsetAsync(scratch, 0, sizeof(int32_t), (cudaStream_t)stream),
+                       "clear no-alloc status")))
+    return rc;
+  return sdemc_price(h_inst, h_cfg, scratch, kNoallocScratchBytes, d_out, d_payoffs, stream);
 }
