@@ -257,7 +257,7 @@ def main():
     need = lib.sdemc_price_scratch_bytes(ctypes.byref(lower(solver, payoff, disc, num_paths=n_target)))
     scratch = N.SCRATCH.get(need, dev)
     out = torch.empty(6, dtype=torch.float64, device=dev)
-    nch = (n_target + 127) // 128
+    nch = (n_target + N.CHUNK_PATHS - 1) // N.CHUNK_PATHS
     base = rank * (1 << 44)
 
     def one_step(i, ev=None):

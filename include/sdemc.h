@@ -26,7 +26,7 @@ extern "C" {
 #define SDEMC_MAX_DIM 8
 #define SDEMC_CHOL_LEN 36       /* packed lower triangle of an 8x8 matrix */
 #define SDEMC_MARK_PARAMS 12
-#define SDEMC_CHUNK_PATHS 128   /* paths per reduction slot: 32 lanes x 4 rounds */
+#define SDEMC_CHUNK_PATHS 32    /* paths per reduction slot: one warp round */
 
 /* ---- status codes ---------------------------------------------------- */
 enum {
@@ -195,7 +195,7 @@ int sdemc_reduce_chunks(void* d_scratch, int64_t nchunks, int width,
  * memory through its own pool, or code that must not call cudaMalloc while
  * it builds a CUDA graph.  The caller passes only d_out (6 doubles, as
  * sdemc_price) and the optional d_payoffs; the scratch is a fixed array of
- * sdemc_price_noalloc_scratch_bytes() (~1.5 MB) inside the library, held on
+ * sdemc_price_noalloc_scratch_bytes() (~6.3 MB) inside the library, held on
  * every GPU that loads the library until the process exits.  Calls with more
  * than SDEMC_NOALLOC_MAX_PATHS paths fail with SDEMC_ENOMEM.  The first call
  * on each device looks up the array's device address (cudaGetSymbolAddress)

@@ -623,47 +623,62 @@ int oracle_mlmc_level(const sdemc_inst* I, int factor, float hf, float hc, int n
   return run_jobs(I, nthreads, 1, factor, hf, hc, ys, out);
 }
 
-/* The GPU's reduction order, restated: FP32 lane sums over 4 rounds, an xor
- * butterfly over 32 lanes per chunk of 128 paths, FP64 chunk partials, then
- * 256 strided FP64 accumulators and a halving tree.  width 3 (price) or 5
- * (MLMC: vals2 holds the second payoff series). out = sums..., mean, var. */
+/* The GPU's reduction order, restated: per chunk of 32 paths (one warp
+ * round) an FP32 xor butterfly of the lane values (0 for paths past n) and of
+ * their squares; FP64 chunk rows; groups of 256 chunks summed by a halving
+ * tree; then 256 strided FP64 accumulators over the group sums and the same
+ * tree.  width 3 (price) or 5 (MLMC: vals2 is the second series).
+ * out = sums..., mean, var. */
+static void chunk_row(const float* vals, const float* vals2, int64_t n, int64_t c, double* row) {
+  float a[32], b[32], e[32], g[32], ta[32], tb[32], te[32], tg[32];
+  int cnt = 0;
+  for (int l = 0; l < 32; ++l) {
+    int64_t p = c * 32 + l;
+    float v = p < n ? vals[p] : 0.f;
+    float w = (p < n && vals2) ? vals2[p] : 0.f;
+    a[l] = v; b[l] = v * v; e[l] = w; g[l] = w * w;
+    cnt += p < n;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    for (int l = 0; l < 32; ++l) {
+      ta[l] = a[l] + a[l ^ o]; tb[l] = b[l] + b[l ^ o]; te[l] = e[l] + e[l ^ o]; tg[l] = g[l] + g[l ^ o];
+    }
+    memcpy(a, ta, sizeof(a)); memcpy(b, tb, sizeof(b)); memcpy(e, te, sizeof(e)); memcpy(g, tg, sizeof(g));
+  }
+  row[0] = (double)a[0]; row[1] = (double)b[0]; row[2] = (double)cnt; row[3] = (double)e[0]; row[4] = (double)g[0];
+}
+
 void oracle_chunk_reduce(const float* vals, const float* vals2, int64_t n, double* out) {
   const int64_t nch = (n + SDEMC_CHUNK_PATHS - 1) / SDEMC_CHUNK_PATHS;
   const int width = vals2 ? 5 : 3;
-  double acc[256][5];
-  memset(acc, 0, sizeof(acc));
-  for (int64_t c = 0; c < nch; ++c) {
-    float ls[32], ls2[32], lf[32], lf2[32];
-    int cnt = 0;
-    for (int l = 0; l < 32; ++l) {
-      ls[l] = 0.f; ls2[l] = 0.f; lf[l] = 0.f; lf2[l] = 0.f;
-      for (int r = 0; r < 4; ++r) {
-        int64_t p = c * 128 + r * 32 + l;
-        if (p < n) {
-          float v = vals[p];
-          ls[l] = ls[l] + v; ls2[l] = ls2[l] + v * v;
-          if (vals2) { float w = vals2[p]; lf[l] = lf[l] + w; lf2[l] = lf2[l] + w * w; }
-          ++cnt;
-        }
-      }
+  const int64_t ngroups = nch > 0 ? (nch + 255) / 256 : 1;
+  double* groups = (double*)calloc((size_t)ngroups * 5, sizeof(double));
+  static double sh[256][5];
+  for (int64_t gi = 0; gi < ngroups; ++gi) {
+    for (int t = 0; t < 256; ++t) {
+      int64_t c = gi * 256 + t;
+      double row[5] = {0, 0, 0, 0, 0};
+      if (c < nch) chunk_row(vals, vals2, n, c, row);
+      for (int w = 0; w < 5; ++w) sh[t][w] = w < width ? row[w] : 0.0;
     }
-    for (int o = 16; o > 0; o >>= 1) {
-      float a[32], b[32], e[32], g[32];
-      for (int l = 0; l < 32; ++l) {
-        a[l] = ls[l] + ls[l ^ o]; b[l] = ls2[l] + ls2[l ^ o];
-        e[l] = lf[l] + lf[l ^ o]; g[l] = lf2[l] + lf2[l ^ o];
-      }
-      memcpy(ls, a, sizeof(a)); memcpy(ls2, b, sizeof(b)); memcpy(lf, e, sizeof(e)); memcpy(lf2, g, sizeof(g));
-    }
-    double row[5] = {(double)ls[0], (double)ls2[0], (double)cnt, (double)lf[0], (double)lf2[0]};
-    int tid = (int)(c % 256);
-    for (int w = 0; w < width; ++w) acc[tid][w] += row[w];
+    for (int o = 128; o > 0; o >>= 1)
+      for (int i = 0; i < o; ++i)
+        for (int w = 0; w < width; ++w) sh[i][w] += sh[i + o][w];
+    for (int w = 0; w < width; ++w) groups[gi * 5 + w] = sh[0][w];
   }
+  for (int t = 0; t < 256; ++t)
+    for (int w = 0; w < 5; ++w) {
+      double acc = 0.0;
+      if (w < width)
+        for (int64_t q = t; q < ngroups; q += 256) acc += groups[q * 5 + w];
+      sh[t][w] = acc;
+    }
   for (int o = 128; o > 0; o >>= 1)
     for (int i = 0; i < o; ++i)
-      for (int w = 0; w < width; ++w) acc[i][w] += acc[i + o][w];
-  for (int w = 0; w < width; ++w) out[w] = acc[0][w];
-  double s = acc[0][0], s2 = acc[0][1], m = acc[0][2];
+      for (int w = 0; w < width; ++w) sh[i][w] += sh[i + o][w];
+  free(groups);
+  for (int w = 0; w < width; ++w) out[w] = sh[0][w];
+  double s = sh[0][0], s2 = sh[0][1], m = sh[0][2];
   out[width] = m > 0 ? s / m : 0.0;
   out[width + 1] = m > 1 ? (s2 - s * s / m) / (m - 1.0) : 0.0;
 }

@@ -17,7 +17,7 @@ LIB_PATH = os.path.join(_HERE, "lib", "libsdemc.so")
 MAX_DIM = 8
 CHOL_LEN = 36
 MARK_PARAMS = 12
-CHUNK_PATHS = 128
+CHUNK_PATHS = 32
 
 # status codes
 OK, EINVAL, EUNSUPPORTED, ENOMEM, ETIMEOUT, ECUDA, EOVERFLOW = range(7)

@@ -68,47 +68,73 @@ int max_iterations(const sdemc_inst* I) {
 }
 
 // ----------------------------------------------------------------- K10 -----
-// One CTA per reduction: thread i adds rows i, i+256, ... in order, then a
-// fixed shared-memory tree.  Bits depend only on the chunk partials.
-constexpr int kRedThreads = 256;
-constexpr int kRedMaxW = 6;
+// Two fixed levels in one launch.  CTA g sums chunks [256g, 256g + 256) with a
+// halving tree into group partial g; the CTA that completes last (completion
+// counter) has thread i add group partials i, i+256, ... in order and runs the
+// same tree, then writes sums, mean, sample variance and the status word and
+// resets the counter.  Which CTA finishes last does not change any bit.
+constexpr int kRedThreads = kGroup;
+constexpr int kRedMaxW = 5;
 
 __global__ void __launch_bounds__(kRedThreads)
-reduce_kernel(const double* __restrict__ part, int64_t nchunks, int width,
-              int32_t* status, double* __restrict__ out) {
+reduce_kernel(const double* __restrict__ part, int64_t nchunks, int width, double* groups,
+              int64_t ngroups, int32_t* status, unsigned* counter, double* __restrict__ out) {
   __shared__ double sh[kRedMaxW][kRedThreads];
+  __shared__ bool last;
+  const int t = threadIdx.x;
+  const int64_t c = (int64_t)blockIdx.x * kRedThreads + t;
+#pragma unroll
+  for (int w = 0; w < kRedMaxW; ++w) sh[w][t] = (w < width && c < nchunks) ? part[c * width + w] : 0.0;
+  __syncthreads();
+  for (int o = kRedThreads / 2; o > 0; o >>= 1) {
+    if (t < o)
+      for (int w = 0; w < width; ++w) sh[w][t] += sh[w][t + o];
+    __syncthreads();
+  }
+  if (t == 0) {
+    for (int w = 0; w < width; ++w) groups[blockIdx.x * width + w] = sh[w][0];
+    __threadfence();
+    last = atomicAdd(counter, 1u) == (unsigned)(ngroups - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
   double acc[kRedMaxW];
 #pragma unroll
   for (int w = 0; w < kRedMaxW; ++w) acc[w] = 0.0;
-  for (int64_t c = threadIdx.x; c < nchunks; c += kRedThreads) {
+  for (int64_t q = t; q < ngroups; q += kRedThreads)
+    for (int w = 0; w < width; ++w) acc[w] += __ldcg(&groups[q * width + w]);
+  __syncthreads();
 #pragma unroll
-    for (int w = 0; w < kRedMaxW; ++w)
-      if (w < width) acc[w] += part[c * width + w];
-  }
-#pragma unroll
-  for (int w = 0; w < kRedMaxW; ++w) sh[w][threadIdx.x] = acc[w];
+  for (int w = 0; w < kRedMaxW; ++w) sh[w][t] = acc[w];
   __syncthreads();
   for (int o = kRedThreads / 2; o > 0; o >>= 1) {
-    if (threadIdx.x < o)
-      for (int w = 0; w < width; ++w) sh[w][threadIdx.x] += sh[w][threadIdx.x + o];
+    if (t < o)
+      for (int w = 0; w < width; ++w) sh[w][t] += sh[w][t + o];
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
+  if (t == 0) {
     const double s = sh[0][0], s2 = sh[1][0], n = sh[2][0];
     for (int w = 0; w < width; ++w) out[w] = sh[w][0];
     // mc_estimates: mean = S/n, var = (S2 - S^2/n)/(n-1)
     out[width] = n > 0 ? s / n : 0.0;
     out[width + 1] = n > 1 ? (s2 - s * s / n) / (n - 1.0) : 0.0;
-    int st = 0;
-    if (status) { st = *status; *status = 0; }
+    const int st = *status;
+    *status = 0;
     out[width + 2] = (double)st;
+    *counter = 0u;
   }
 }
 
-int launch_reduce(const double* part, int64_t nchunks, int width, int32_t* status,
-                  double* out, cudaStream_t s) {
+int launch_reduce(void* scratch, int64_t nchunks, int width, double* out, cudaStream_t s) {
   if (width < 3 || width > kRedMaxW) return fail(SDEMC_EINVAL, "reduce width %d", width);
-  reduce_kernel<<<1, kRedThreads, 0, s>>>(part, nchunks, width, status, out);
+  const int64_t ngroups = num_groups_for(nchunks);
+  if (ngroups > 0x7fffffff) return fail(SDEMC_EINVAL, "too many chunks");
+  double* part = scratch_chunks(scratch);
+  double* groups = part + nchunks * width;
+  reduce_kernel<<<(unsigned)ngroups, kRedThreads, 0, s>>>(part, nchunks, width, groups, ngroups,
+                                                          scratch_status(scratch), scratch_counter(scratch),
+                                                          out);
   return check_cuda(cudaGetLastError(), "reduce_kernel launch");
 }
 
@@ -116,8 +142,9 @@ __global__ void philox_kernel(uint64_t seed, uint32_t stream_id, uint32_t tag, u
                               uint32_t first, int n, uint32_t* out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  StreamKey k;
-  k.init(seed, stream_id, path);
+  const RoundKeys rk = make_round_keys(seed);
+  PathStream k;
+  k.init(&rk, stream_id, path);
   const U4 w = k.block(tag, first + (uint32_t)i);
   out[4 * i + 0] = w.x; out[4 * i + 1] = w.y; out[4 * i + 2] = w.z; out[4 * i + 3] = w.w;
 }

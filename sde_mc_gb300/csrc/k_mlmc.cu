@@ -73,49 +73,45 @@ SDEMC_DI void simulate_pair(const sdemc_inst& I, Draws& dr, int factor, float hf
     if (act && jump_due(nj, tf)) {
       float J;
       int sel;
-      dr.jump_mark(kc, J, sel);
+      nj = dr.on_fire(I, kc, nj, J, sel);
       apply_jump<D, EXACT>(I, xf, I.exact_jumps ? xf : oldf, J, sel);
       apply_jump<D, EXACT>(I, xc, I.exact_jumps ? xc : oldc, J, sel);
-      nj = dr.jump_next(I, nj);
     }
     ++kc;
     act = tf < T;
+    dr.after_step(I, kc, nj, act);
   }
 }
 
+struct LevelParams {
+  sdemc_inst I;
+  RoundKeys rk;
+};
+
 template <int D, int NOISE>
 __global__ void __launch_bounds__(128)
-mlmc_kernel(const __grid_constant__ sdemc_inst I, int factor, float hf, float hc,
+mlmc_kernel(const __grid_constant__ LevelParams P, int factor, float hf, float hc,
             double* __restrict__ part, float* __restrict__ yout, int32_t* __restrict__ status,
             int64_t nchunks, int max_iters) {
+  const sdemc_inst& I = P.I;
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   bool ovf = false;
   for (int64_t c = warp; c < nchunks; c += nwarps) {
-    float s = 0.f, s2 = 0.f, f = 0.f, f2 = 0.f;
-    int n = 0;
-#pragma unroll 1
-    for (int r = 0; r < kChunk / 32; ++r) {
-      const int64_t p = c * kChunk + r * 32 + lane;
-      NativeDraws<D, NOISE> dr;
-      dr.init(I, (uint64_t)p);
-      float xf[D], xc[D];
-      simulate_pair<D, NOISE, false>(I, dr, factor, hf, hc, xf, xc, max_iters, ovf);
-      const float pf = payoff<D>(I, xf), pc = payoff<D>(I, xc);
-      const float Y = __fmul_rn(I.discount, __fsub_rn(pf, pc));
-      const float F = __fmul_rn(pf, I.discount);
-      if (p < I.num_paths) {
-        s = __fadd_rn(s, Y);
-        s2 = __fadd_rn(s2, __fmul_rn(Y, Y));
-        f = __fadd_rn(f, F);
-        f2 = __fadd_rn(f2, __fmul_rn(F, F));
-        ++n;
-        if (yout) yout[p] = Y;
-      }
-    }
-    s = warp_sum(s); s2 = warp_sum(s2); f = warp_sum(f); f2 = warp_sum(f2);
-    n = __reduce_add_sync(kFull, n);
+    const int64_t p = c * kChunk + lane;
+    NativeDraws<D, NOISE> dr;
+    dr.init(I, (uint64_t)p, &P.rk);
+    float xf[D], xc[D];
+    simulate_pair<D, NOISE, false>(I, dr, factor, hf, hc, xf, xc, max_iters, ovf);
+    const bool valid = p < I.num_paths;
+    const float pf = payoff<D>(I, xf), pc = payoff<D>(I, xc);
+    const float Y = valid ? __fmul_rn(I.discount, __fsub_rn(pf, pc)) : 0.f;
+    const float F = valid ? __fmul_rn(pf, I.discount) : 0.f;
+    if (valid && yout) yout[p] = Y;
+    const float s = warp_sum(Y), s2 = warp_sum(__fmul_rn(Y, Y));
+    const float f = warp_sum(F), f2 = warp_sum(__fmul_rn(F, F));
+    const int n = __popc(__ballot_sync(kFull, valid));
     if (lane == 0) {
       double* o = part + c * 5;
       o[0] = (double)s; o[1] = (double)s2; o[2] = (double)n; o[3] = (double)f; o[4] = (double)f2;
@@ -152,11 +148,12 @@ mlmc_replay_kernel(const __grid_constant__ sdemc_inst I, int factor, float hf, f
 
 template <int D, int NOISE>
 __global__ void __launch_bounds__(128)
-mlmc_terminals_kernel(const __grid_constant__ sdemc_inst I, int factor, float hf, float hc,
+mlmc_terminals_kernel(const __grid_constant__ LevelParams P, int factor, float hf, float hc,
                       float* xf_out, float* xc_out, int32_t* status, int max_iters) {
+  const sdemc_inst& I = P.I;
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   NativeDraws<D, NOISE> dr;
-  dr.init(I, (uint64_t)p);
+  dr.init(I, (uint64_t)p, &P.rk);
   bool ovf = false;
   float xf[D], xc[D];
   simulate_pair<D, NOISE, false>(I, dr, factor, hf, hc, xf, xc, max_iters, ovf);
@@ -181,7 +178,7 @@ using namespace sdemc;
 
 extern "C" size_t sdemc_mlmc_scratch_bytes(const sdemc_inst* h_inst) {
   if (!h_inst) return 0;
-  return kScratchHeader + (size_t)num_chunks(h_inst) * 5 * sizeof(double);
+  return scratch_bytes_for(num_chunks(h_inst), 5);
 }
 
 extern "C" int sdemc_mlmc_level(const sdemc_inst* h_inst, int fine, int coarse, float h_fine,
@@ -199,11 +196,14 @@ extern "C" int sdemc_mlmc_level(const sdemc_inst* h_inst, int fine, int coarse, 
   sdemc_inst I = *h_inst;
   I.num_steps = coarse;  // iteration cap counts coarse steps
   cudaStream_t s = (cudaStream_t)stream;
-  int32_t* status = (int32_t*)d_scratch;
-  double* part = (double*)((char*)d_scratch + kScratchHeader);
+  int32_t* status = scratch_status(d_scratch);
+  double* part = scratch_chunks(d_scratch);
   const int64_t nch = num_chunks(h_inst);
   const int factor = fine / coarse;
   const int mi = max_iterations(&I);
+  LevelParams P;
+  P.I = I;
+  P.rk = make_round_keys(I.seed);
   if (nch > 0) {
     const int threads = cfg.block_threads > 0 ? cfg.block_threads : 128;
 #define SDEMC_MLMC_CASE(D_, N_)                                                                  \
@@ -218,13 +218,13 @@ extern "C" int sdemc_mlmc_level(const sdemc_inst* h_inst, int fine, int coarse, 
     int64_t ctas = (nch + threads / 32 - 1) / (threads / 32);                                    \
     const int64_t resident = (int64_t)num_sms() * per_sm;                                        \
     if (ctas > resident) ctas = resident;                                                        \
-    kern<<<(unsigned)ctas, threads, 0, s>>>(I, factor, h_fine, h_coarse, part, d_y, status, nch, mi); \
+    kern<<<(unsigned)ctas, threads, 0, s>>>(P, factor, h_fine, h_coarse, part, d_y, status, nch, mi); \
   }
     SDEMC_DISPATCH(I.dim, I.noise, SDEMC_MLMC_CASE)
 #undef SDEMC_MLMC_CASE
     if ((rc = check_cuda(cudaGetLastError(), "mlmc_kernel launch"))) return rc;
   }
-  return launch_reduce(part, nch, 5, status, d_out, s);
+  return launch_reduce(d_scratch, nch, 5, d_out, s);
 }
 
 extern "C" int sdemc_mlmc_replay(const sdemc_inst* h_inst, int fine, int coarse, float h_fine,
@@ -268,8 +268,11 @@ extern "C" int sdemc_mlmc_terminals(const sdemc_inst* h_inst, int fine, int coar
   const unsigned blocks = (unsigned)((I.num_paths + 127) / 128);
   const int factor = fine / coarse;
   const int mi = max_iterations(&I);
+  LevelParams P;
+  P.I = I;
+  P.rk = make_round_keys(I.seed);
 #define SDEMC_MLMC_TERM_CASE(D_, N_)                                               \
-  mlmc_terminals_kernel<D_, N_><<<blocks, 128, 0, s>>>(I, factor, h_fine, h_coarse, \
+  mlmc_terminals_kernel<D_, N_><<<blocks, 128, 0, s>>>(P, factor, h_fine, h_coarse, \
                                                        d_xf, d_xc, d_status, mi);
   SDEMC_DISPATCH(I.dim, I.noise, SDEMC_MLMC_TERM_CASE)
 #undef SDEMC_MLMC_TERM_CASE

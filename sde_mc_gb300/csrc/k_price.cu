@@ -3,11 +3,11 @@
 // Stands in for mc_simple (sde_mc/mc.py:53-123) driving JumpDiffusionSolver
 // .solve (sde_mc/solvers.py:164-226) or DiffusionSolver.solve (:68-88) and
 // Option.__call__ (sde_mc/options.py:175-176).  Nothing path-shaped touches
-// HBM: each lane keeps its path in registers, draws its increments from its
-// own Philox stream, and folds its discounted payoff into FP32 lane sums.
-// A chunk of SDEMC_CHUNK_PATHS consecutive paths (32 lanes x 4 rounds) is
-// reduced by a fixed warp butterfly and stored as (sum, sum_sq, n) in FP64 at
-// its own slot, so the bits never depend on the grid shape.
+// HBM: each lane keeps its path in registers and draws its increments from its
+// own Philox stream.  A chunk of SDEMC_CHUNK_PATHS = 32 consecutive paths (one
+// warp round) is reduced by a fixed xor butterfly in FP32 and stored as
+// (sum, sum_sq, n) in FP64 at its own slot, so the bits never depend on the
+// grid shape; K10 then sums the slots in a fixed order.
 #include <mutex>
 
 #include "sdemc_device.cuh"
@@ -15,37 +15,35 @@
 
 namespace sdemc {
 
-template <int D, int NOISE, bool EXACT>
+struct PriceParams {
+  sdemc_inst I;
+  RoundKeys rk;
+};
+
+template <int D, int NOISE, int MODE>
 __global__ void __launch_bounds__(256)
-price_kernel(const __grid_constant__ sdemc_inst I, double* __restrict__ part,
-             float* __restrict__ payoffs, int32_t* __restrict__ status,
-             int64_t nchunks, int max_iters) {
+price_kernel(const __grid_constant__ PriceParams P, double* __restrict__ part,
+             float* __restrict__ payoffs, int32_t* __restrict__ status, int64_t nchunks,
+             int max_iters) {
+  const sdemc_inst& I = P.I;
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   bool ovf = false;
   for (int64_t c = warp; c < nchunks; c += nwarps) {
-    float s = 0.f, s2 = 0.f;
-    int n = 0;
-#pragma unroll 1
-    for (int r = 0; r < kChunk / 32; ++r) {
-      const int64_t p = c * kChunk + r * 32 + lane;
-      NativeDraws<D, NOISE> dr;
-      dr.init(I, (uint64_t)p);
-      NullSink sk;
-      float x[D];
-      simulate<D, NOISE, EXACT>(I, dr, sk, x, max_iters, ovf);
-      const float P = __fmul_rn(payoff<D>(I, x), I.discount);
-      if (p < I.num_paths) {
-        s = __fadd_rn(s, P);
-        s2 = __fadd_rn(s2, __fmul_rn(P, P));
-        ++n;
-        if (payoffs) payoffs[p] = P;
-      }
-    }
-    s = warp_sum(s);
-    s2 = warp_sum(s2);
-    n = __reduce_add_sync(kFull, n);
+    const int64_t p = c * kChunk + lane;
+    NativeDraws<D, NOISE> dr;
+    dr.init(I, (uint64_t)p, &P.rk);
+    NullSink sk;
+    float x[D];
+    simulate<D, NOISE, MODE>(I, dr, sk, x, max_iters, ovf);
+    const bool valid = p < I.num_paths;
+    const float pay = __fmul_rn(payoff<D>(I, x), I.discount);
+    const float v = valid ? pay : 0.f;
+    if (valid && payoffs) payoffs[p] = pay;
+    const float s = warp_sum(v);
+    const float s2 = warp_sum(__fmul_rn(v, v));
+    const int n = __popc(__ballot_sync(kFull, valid));
     if (lane == 0) {
       part[c * 3 + 0] = (double)s;
       part[c * 3 + 1] = (double)s2;
@@ -55,10 +53,10 @@ price_kernel(const __grid_constant__ sdemc_inst I, double* __restrict__ part,
   if (ovf) atomicOr(status, SDEMC_EOVERFLOW);
 }
 
-template <int D, int NOISE, bool EXACT>
+template <int D, int NOISE, int MODE>
 static int launch_price_t(const sdemc_inst& I, const sdemc_cfg& cfg, double* part,
                           float* payoffs, int32_t* status, int64_t nchunks, cudaStream_t s) {
-  auto kern = price_kernel<D, NOISE, EXACT>;
+  auto kern = price_kernel<D, NOISE, MODE>;
   const int threads = cfg.block_threads > 0 ? cfg.block_threads : 128;
   int per_sm = 0;
   int rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0),
@@ -71,7 +69,10 @@ static int launch_price_t(const sdemc_inst& I, const sdemc_cfg& cfg, double* par
   int64_t ctas = (nchunks + warps_per_cta - 1) / warps_per_cta;
   if (ctas > resident) ctas = resident;
   if (ctas < 1) ctas = 1;
-  kern<<<(unsigned)ctas, threads, 0, s>>>(I, part, payoffs, status, nchunks, max_iterations(&I));
+  PriceParams P;
+  P.I = I;
+  P.rk = make_round_keys(I.seed);
+  kern<<<(unsigned)ctas, threads, 0, s>>>(P, part, payoffs, status, nchunks, max_iterations(&I));
   return check_cuda(cudaGetLastError(), "price_kernel launch");
 }
 
@@ -81,7 +82,7 @@ using namespace sdemc;
 
 extern "C" size_t sdemc_price_scratch_bytes(const sdemc_inst* h_inst) {
   if (!h_inst) return 0;
-  return kScratchHeader + (size_t)num_chunks(h_inst) * 3 * sizeof(double);
+  return scratch_bytes_for(num_chunks(h_inst), 3);
 }
 
 extern "C" int sdemc_price_chunks(const sdemc_inst* h_inst, const sdemc_cfg* h_cfg, void* d_scratch,
@@ -98,14 +99,19 @@ extern "C" int sdemc_price_chunks(const sdemc_inst* h_inst, const sdemc_cfg* h_c
   if (h_cfg) cfg = *h_cfg;
   const sdemc_inst& I = *h_inst;
   cudaStream_t s = (cudaStream_t)stream;
-  int32_t* status = (int32_t*)d_scratch;
-  double* part = (double*)((char*)d_scratch + kScratchHeader);
+  int32_t* status = scratch_status(d_scratch);
+  double* part = scratch_chunks(d_scratch);
   const int64_t nch = num_chunks(h_inst);
   if (nch == 0) return SDEMC_OK;
   const bool exact = (cfg.flags & SDEMC_CFG_EXACT_EULER) != 0;
-#define SDEMC_PRICE_CASE(D_, N_)                                                              \
-  rc = exact ? launch_price_t<D_, N_, true>(I, cfg, part, d_payoffs, status, nch, s)          \
-             : launch_price_t<D_, N_, false>(I, cfg, part, d_payoffs, status, nch, s);
+  const bool nominal = (I.flags & SDEMC_INST_PAYOFF_AT_NOMINAL_STEP) != 0;
+#define SDEMC_PRICE_CASE(D_, N_)                                                                   \
+  rc = nominal ? (exact ? launch_price_t<D_, N_, kModeExact | kModeNominal>(I, cfg, part, d_payoffs, \
+                                                                          status, nch, s)          \
+                        : launch_price_t<D_, N_, kModeNominal>(I, cfg, part, d_payoffs, status,   \
+                                                               nch, s))                           \
+               : (exact ? launch_price_t<D_, N_, kModeExact>(I, cfg, part, d_payoffs, status, nch, s) \
+                        : launch_price_t<D_, N_, 0>(I, cfg, part, d_payoffs, status, nch, s));
   SDEMC_DISPATCH(I.dim, I.noise, SDEMC_PRICE_CASE)
 #undef SDEMC_PRICE_CASE
   return rc;
@@ -114,9 +120,7 @@ extern "C" int sdemc_price_chunks(const sdemc_inst* h_inst, const sdemc_cfg* h_c
 extern "C" int sdemc_reduce_chunks(void* d_scratch, int64_t nchunks, int width, double* d_out,
                                    void* stream) {
   if (!d_scratch || !d_out || nchunks < 0) return fail(SDEMC_EINVAL, "bad reduce args");
-  int32_t* status = (int32_t*)d_scratch;
-  double* part = (double*)((char*)d_scratch + kScratchHeader);
-  return launch_reduce(part, nchunks, width, status, d_out, (cudaStream_t)stream);
+  return launch_reduce(d_scratch, nchunks, width, d_out, (cudaStream_t)stream);
 }
 
 extern "C" int sdemc_price(const sdemc_inst* h_inst, const sdemc_cfg* h_cfg, void* d_scratch,
@@ -135,14 +139,15 @@ extern "C" int sdemc_price(const sdemc_inst* h_inst, const sdemc_cfg* h_cfg, voi
 // would fail or fragment it), code running inside a CUDA graph it is building,
 // or a plugin whose host forbids allocations from third-party code.  Those
 // callers still pass their inputs and outputs, but cannot provide scratch.
-// sdemc_price_noalloc keeps the per-chunk partials and the status word in the
-// array below, which lives in this library's module: every GPU that loads the
-// library holds kNoallocScratchBytes (about 1.5 MB) of it until the process
-// exits.  The limit is SDEMC_NOALLOC_MAX_PATHS paths per call.
+// sdemc_price_noalloc keeps the per-chunk partials, the status word and the
+// reduction's completion counter in the array below, which lives in this
+// library's module: every GPU that loads the library holds
+// kNoallocScratchBytes (about 6.3 MB) of it until the process exits.  The
+// limit is SDEMC_NOALLOC_MAX_PATHS paths per call.
 // ---------------------------------------------------------------------------
 static constexpr int64_t kNoallocMaxChunks =
     ((int64_t)SDEMC_NOALLOC_MAX_PATHS + kChunk - 1) / kChunk;
-static constexpr size_t kNoallocScratchBytes = kScratchHeader + (size_t)kNoallocMaxChunks * 3 * sizeof(double);
+static constexpr size_t kNoallocScratchBytes = scratch_bytes_for(kNoallocMaxChunks, 3);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
 
@@ -181,9 +186,9 @@ extern "C" int sdemc_price_noalloc(const sdemc_inst* h_inst, const sdemc_cfg* h_
                 (long long)h_inst->num_paths, SDEMC_NOALLOC_MAX_PATHS);
   void* scratch = nullptr;
   if ((rc = noalloc_scratch_address(&scratch))) return rc;
-  // The array keeps the previous call's contents: the status word must start
-  // at zero (the chunk partials are all rewritten by this call).
-  if ((rc = check_cuda(cudaMemsetAsync(scratch, 0, sizeof(int32_t), (cudaStream_t)stream),
+  // The array keeps the previous call's contents: the status word and the
+  // completion counter must start at zero (the partials are all rewritten).
+  if ((rc = check_cuda(cudaMemsetAsync(scratch, 0, 2 * sizeof(int32_t), (cudaStream_t)stream),
                        "clear no-alloc status")))
     return rc;
   return sdemc_price(h_inst, h_cfg, scratch, kNoallocScratchBytes, d_out, d_payoffs, stream);

@@ -11,13 +11,19 @@
 
 namespace sdemc {
 
-template <int D, int NOISE, bool EXACT>
+struct StoreParams {
+  sdemc_inst I;
+  RoundKeys rk;
+};
+
+template <int D, int NOISE, int MODE>
 __global__ void __launch_bounds__(128)
-materialise_kernel(const __grid_constant__ sdemc_inst I, int S, float* paths, float* left,
+materialise_kernel(const __grid_constant__ StoreParams P, int S, float* paths, float* left,
                    float* time, float* jumps, float* normals, float* payoffs, int32_t* steps,
                    float* zout, int zdim, float* jt, float* jm, int32_t* jsel, int jcap,
                    int32_t* status, int max_iters) {
   using L = Layout<D, NOISE>;
+  const sdemc_inst& I = P.I;
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = p < I.num_paths;
   StoreSink sk{};
@@ -33,26 +39,28 @@ materialise_kernel(const __grid_constant__ sdemc_inst I, int S, float* paths, fl
     sk.z = zout ? zout + (size_t)p * S * zdim : nullptr;
   }
   NativeDraws<D, NOISE> dr;
-  dr.init(I, (uint64_t)p);
+  dr.init(I, (uint64_t)p, &P.rk);
   bool ovf = false;
   float x[D];
   const int it = max_iters < S ? max_iters : S;
-  const int own = simulate<D, NOISE, EXACT>(I, dr, sk, x, it, ovf);
+  const int own = simulate<D, NOISE, MODE>(I, dr, sk, x, it, ovf);
   if (!valid) return;
   if (payoffs) payoffs[p] = __fmul_rn(payoff<D>(I, x), I.discount);
   if (steps) steps[p] = own;
   if (ovf) atomicOr(status, SDEMC_EOVERFLOW);
-  // Export the jump stream (times, marks, picks) for the oracle: it is a pure
-  // function of the path's counter, so regenerate it here.
+  // Export the jump stream (times, marks, picks) for the oracle: blocks 0, 1,
+  // 2, ... of the path's jump stream, times accumulated as the loop does.
   if (jcap > 0 && (jt || jm || jsel)) {
-    NativeDraws<D, NOISE> j2;
-    j2.init(I, (uint64_t)p);
-    float nj = j2.jump_first(I);
+    float nj = inf_f();
     for (int j = 0; j < jcap; ++j) {
+      JumpDraw d{0.f, 0.f, 0};
+      if (I.rate > 0.f) {
+        d = jump_from_block<D>(I, dr.ps.block(kTagJumps, (uint32_t)j));
+        nj = j == 0 ? d.gap : __fadd_rn(nj, d.gap);
+      }
       if (jt) jt[(size_t)p * jcap + j] = nj;
-      if (jm) jm[(size_t)p * jcap + j] = j2.jmark;
-      if (jsel) jsel[(size_t)p * jcap + j] = j2.jsel;
-      if (I.rate > 0.f) nj = j2.jump_next(I, nj);
+      if (jm) jm[(size_t)p * jcap + j] = d.mark;
+      if (jsel) jsel[(size_t)p * jcap + j] = d.sel;
     }
   }
 }
@@ -88,7 +96,7 @@ replay_kernel(const __grid_constant__ sdemc_inst I, int bs, int S, int MJ, const
   dr.overflow = false;
   bool ovf = false;
   float x[D];
-  const int own = simulate<D, NOISE, true>(I, dr, sk, x, S, ovf);
+  const int own = simulate<D, NOISE, kModeExact>(I, dr, sk, x, S, ovf);
   if (!valid) return;
   if (payoffs) payoffs[p] = __fmul_rn(payoff<D>(I, x), I.discount);
   if (steps) steps[p] = own;
@@ -115,13 +123,17 @@ extern "C" int sdemc_materialise(const sdemc_inst* h_inst, int steps_cap, float*
   const unsigned blocks = (unsigned)((I.num_paths + 127) / 128);
   cudaStream_t s = (cudaStream_t)stream;
   const int mi = max_iterations(&I);
+  StoreParams P;
+  P.I = I;
+  P.rk = make_round_keys(I.seed);
+  const bool nominal = (I.flags & SDEMC_INST_PAYOFF_AT_NOMINAL_STEP) != 0;
 #define SDEMC_MAT_CASE(D_, N_)                                                                   \
   {                                                                                              \
     constexpr int ZD = Layout<D_, N_>::ZD;                                                       \
     if (d_z && zdim != ZD) return fail(SDEMC_EINVAL, "zdim %d != %d for this layout", zdim, ZD); \
-    materialise_kernel<D_, N_, false><<<blocks, 128, 0, s>>>(                                    \
-        I, steps_cap, d_paths, d_left, d_time, d_jumps, d_normals, d_payoffs, d_steps, d_z,     \
-        ZD, d_jt, d_jm, d_jsel, jcap, d_status, mi);                                             \
+    auto kern = nominal ? materialise_kernel<D_, N_, kModeNominal> : materialise_kernel<D_, N_, 0>; \
+    kern<<<blocks, 128, 0, s>>>(P, steps_cap, d_paths, d_left, d_time, d_jumps, d_normals,      \
+                                d_payoffs, d_steps, d_z, ZD, d_jt, d_jm, d_jsel, jcap, d_status, mi); \
   }
   SDEMC_DISPATCH(I.dim, I.noise, SDEMC_MAT_CASE)
 #undef SDEMC_MAT_CASE

@@ -3,6 +3,8 @@
 //  * Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as
 //    easy as 1, 2, 3", SC'11), written from the paper; counter-based, so any
 //    path's draws are a pure function of (seed, stream, path index, block).
+//    The ten round keys depend on the seed only and are precomputed per
+//    launch, so the kernels read them as constants.
 //  * Box-Muller normals on MUFU intrinsics (__logf, rsqrtf, __sinf/__cosf).
 //  * The reference's jump-adapted Euler loop (sde_mc/solvers.py:164-226) with
 //    its exact float32 grid arithmetic, written with _rn intrinsics so that no
@@ -16,6 +18,7 @@
 namespace sdemc {
 
 #define SDEMC_DI __device__ __forceinline__
+#define SDEMC_HDI __host__ __device__ __forceinline__
 constexpr unsigned kFull = 0xffffffffu;
 constexpr float kTwoPi = 6.283185307179586f;
 constexpr float kPi = 3.141592653589793f;
@@ -23,14 +26,25 @@ constexpr float kPi = 3.141592653589793f;
 // ---------------------------------------------------------------- Philox ----
 struct U4 { uint32_t x, y, z, w; };
 
-SDEMC_DI U4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
-                          uint32_t k0, uint32_t k1) {
+// Round r of Philox4x32-10 uses key (k0 + r*0x9E3779B9, k1 + r*0xBB67AE85).
+struct RoundKeys { uint32_t k[20]; };
+
+SDEMC_HDI RoundKeys make_round_keys(uint64_t seed) {
+  RoundKeys rk;
+  uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  for (int r = 0; r < 10; ++r) {
+    rk.k[2 * r] = k0; rk.k[2 * r + 1] = k1;
+    k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+  }
+  return rk;
+}
+
+SDEMC_DI U4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, const RoundKeys& rk) {
 #pragma unroll
   for (int r = 0; r < 10; ++r) {
-    if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
     const uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
     const uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
-    const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    const uint32_t n0 = hi1 ^ c1 ^ rk.k[2 * r], n2 = hi0 ^ c3 ^ rk.k[2 * r + 1];
     c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
   }
   return U4{c0, c1, c2, c3};
@@ -52,15 +66,19 @@ SDEMC_DI float bm_angle(uint32_t wb) { return __fmaf_rn(kTwoPi, u01(wb), -kPi); 
 constexpr uint32_t kTagDiffusion = 0u;
 constexpr uint32_t kTagJumps = 1u;
 
-struct StreamKey {
-  uint32_t k0, k1, c1, c2base, c3;
-  SDEMC_DI void init(uint64_t seed, uint32_t stream_id, uint64_t gpath) {
-    k0 = (uint32_t)seed; k1 = (uint32_t)(seed >> 32);
-    c1 = (uint32_t)gpath; c2base = (uint32_t)(gpath >> 32) & 0xFFFFu;
+// Counter words of one path: c1 = path low word, c2 = path high 16 bits |
+// tag << 16, c3 = stream id; c0 is the block index.
+struct PathStream {
+  const RoundKeys* rk;
+  uint32_t c1, c2base, c3;
+  SDEMC_DI void init(const RoundKeys* keys, uint32_t stream_id, uint64_t gpath) {
+    rk = keys;
+    c1 = (uint32_t)gpath;
+    c2base = (uint32_t)(gpath >> 32) & 0xFFFFu;
     c3 = stream_id;
   }
   SDEMC_DI U4 block(uint32_t tag, uint32_t b) const {
-    return philox4x32_10(b, c1, c2base | (tag << 16), c3, k0, k1);
+    return philox4x32_10(b, c1, c2base | (tag << 16), c3, *rk);
   }
 };
 
@@ -69,10 +87,8 @@ template <int D, int NOISE> struct Layout {
   // normals per step drawn from the diffusion stream
   static constexpr int ZD = NOISE == SDEMC_NOISE_DIAG ? D
                           : NOISE == SDEMC_NOISE_INDEP_SHARED ? D + 1 : 2 * D;
-  // slots per step: tight when ZD divides 4, else whole Philox blocks
-  static constexpr int SLOTS = (ZD == 1 || ZD == 2 || ZD == 4) ? ZD : 4 * ((ZD + 3) / 4);
-  static constexpr int NB = (ZD + 3) / 4;                 // blocks per step (ZD>2)
-  static constexpr int NW = NOISE == SDEMC_NOISE_DIAG ? 1 : 2;  // noise columns
+  static constexpr int NB = (ZD + 3) / 4;                        // blocks per step (ZD > 2)
+  static constexpr int NW = NOISE == SDEMC_NOISE_DIAG ? 1 : 2;   // noise columns
 };
 
 SDEMC_DI float chol_at(const sdemc_inst& I, int i, int j) { return I.chol[i * (i + 1) / 2 + j]; }
@@ -94,25 +110,78 @@ SDEMC_DI void correlate(const sdemc_inst& I, const float* z, float sq, float* dW
   }
 }
 
+// InverseCdf.__call__ (sde_mc/levy.py:22-30): piecewise inverse of the
+// truncated two-sided tempered-stable jump measure.  mark_p = cm, cp, mu,
+// alpha, eps, lda, y1, y2, y3, shift, eps^-alpha, -1/alpha.
+SDEMC_DI float inverse_cdf(const sdemc_inst& I, float y) {
+  const float cm = I.mark_p[0], cp = I.mark_p[1], mu = I.mark_p[2], al = I.mark_p[3];
+  const float lda = I.mark_p[5], y1 = I.mark_p[6], y2 = I.mark_p[7], y3 = I.mark_p[8];
+  const float epa = I.mark_p[10], nia = I.mark_p[11];
+  if (y <= y1) return logf((mu * lda * y) / cm) / mu - 1.0f;
+  if (y < y2) return -powf(al * ((lda * y / cm) - (1.0f / mu)) + 1.0f, nia);
+  if (y < y3) return powf((-al / cp) * (lda * y - cm / mu - cm * ((epa - 1.0f) / al)) + epa, nia);
+  return 1.0f - (1.0f / mu) * logf(mu * lda * (1.0f - y) / cp);
+}
+
+// One jump-stream block: x -> exponential gap, y (,z) -> lognormal mark (Box-
+// Muller cosine branch) or the inverse-CDF uniform, w -> asset pick.
+struct JumpDraw { float gap, mark; int sel; };
+
+template <int D>
+SDEMC_DI JumpDraw jump_from_block(const sdemc_inst& I, U4 w) {
+  JumpDraw j;
+  j.gap = -logf(u01(w.x)) * I.inv_rate;
+  if (I.mark == SDEMC_MARK_LOGNORMAL) {
+    const float zn = bm_radius(w.y) * __cosf(bm_angle(w.z));
+    j.mark = expf(I.mark_p[1] * zn + I.mark_p[0]) - 1.0f;
+  } else if (I.mark == SDEMC_MARK_INVCDF) {
+    j.mark = inverse_cdf(I, u01(w.y) + I.mark_p[9]);
+  } else {
+    j.mark = 0.f;
+  }
+  j.sel = 0;
+  if (I.jump_target == SDEMC_JUMP_ONE_ASSET) {
+    const float us = u01(w.w);
+#pragma unroll
+    for (int i = 0; i < D - 1; ++i) j.sel += (us >= I.jump_cdf[i]) ? 1 : 0;
+  }
+  return j;
+}
+
+SDEMC_DI float inf_f() { return __int_as_float(0x7f800000); }
+
 // ------------------------------------------------------------- draws -------
 // Native draws: counter-based Philox streams of one path.
+//
+// Jump stream: every lane holds the next jump (time nj, mark, asset) and one
+// reserve jump (gap, mark, asset; gap < 0 when empty).  Firing uses the held
+// jump and promotes the reserve — a few instructions in the divergent branch.
+// Reserves are refilled by the whole warp at once (after_step): the w-th lane
+// that needs a block computes it for the w-th requester and hands it back
+// through shuffles, so one pass with all lanes busy serves many lanes.  The
+// jump times, marks and picks are those of blocks 0, 1, 2, ... of the path's
+// jump stream, whichever lane computes them.
+constexpr int kRefillBatch = 8;
+constexpr int kRefillEvery = 4;
+
 template <int D, int NOISE>
 struct NativeDraws {
   using L = Layout<D, NOISE>;
-  StreamKey key;
-  float buf[4];        // buffered normals when ZD in {1,2}
-  uint32_t jblock;     // jump-stream block of the pending jump
-  float jmark;         // mark of the pending jump
-  int jsel;            // asset of the pending jump (ONE_ASSET)
-  float sq_h, h_nom;   // cached sqrt of the nominal step
+  PathStream ps;
+  float buf[4];          // buffered normals when ZD in {1,2}
+  float sq_h, h_nom;     // cached sqrt of the nominal step
+  float cur_mark, res_gap, res_mark;
+  uint32_t jblk;         // next jump-stream block to draw
+  int cur_sel, res_sel;
 
-  SDEMC_DI void init(const sdemc_inst& I, uint64_t gpath) {
-    key.init(I.seed, I.stream_id, I.path_offset + gpath);
-    h_nom = I.h; sq_h = sqrtf(I.h);
+  SDEMC_DI void init(const sdemc_inst& I, uint64_t gpath, const RoundKeys* rk) {
+    ps.init(rk, I.stream_id, I.path_offset + gpath);
+    h_nom = I.h;
+    sq_h = sqrtf(I.h);
   }
 
   SDEMC_DI void fill4(uint32_t b, float* o) const {
-    const U4 w = key.block(kTagDiffusion, b);
+    const U4 w = ps.block(kTagDiffusion, b);
     const float r0 = bm_radius(w.x), a0 = bm_angle(w.y);
     const float r1 = bm_radius(w.z), a1 = bm_angle(w.w);
     o[0] = r0 * __cosf(a0); o[1] = r0 * __sinf(a0);
@@ -145,7 +214,8 @@ struct NativeDraws {
   // Step increments for step k of length dt.
   SDEMC_DI void increments(const sdemc_inst& I, int k, float dt, float* dW, float* dW2, float* z) {
     normals(k, z);
-    const float sq = (dt == h_nom) ? sq_h : sqrtf(dt);
+    float sq = sq_h;
+    if (dt != h_nom) sq = sqrtf(dt);
     correlate<D>(I, z, sq, dW);
     if (NOISE == SDEMC_NOISE_INDEP_SHARED) {
       const float s = __fmul_rn(z[D], sq);
@@ -156,54 +226,63 @@ struct NativeDraws {
     }
   }
 
-  // Jump stream block j: x -> exponential gap, (y, z) -> lognormal mark or the
-  // inverse-CDF uniform, w -> asset pick.
-  SDEMC_DI float load_jump(const sdemc_inst& I, uint32_t j) {
-    const U4 w = key.block(kTagJumps, j);
-    const float gap = -logf(u01(w.x)) * I.inv_rate;
-    if (I.mark == SDEMC_MARK_LOGNORMAL) {
-      const float zn = bm_radius(w.y) * __cosf(bm_angle(w.z));
-      jmark = expf(I.mark_p[1] * zn + I.mark_p[0]) - 1.0f;
-    } else if (I.mark == SDEMC_MARK_INVCDF) {
-      jmark = inverse_cdf(I, u01(w.y) + I.mark_p[9]);
-    } else {
-      jmark = 0.f;
-    }
-    jsel = 0;
-    if (I.jump_target == SDEMC_JUMP_ONE_ASSET) {
-      const float us = u01(w.w);
-#pragma unroll
-      for (int i = 0; i < D - 1; ++i) jsel += (us >= I.jump_cdf[i]) ? 1 : 0;
-    }
-    return gap;
-  }
-
-  // InverseCdf.__call__ (sde_mc/levy.py:22-30): piecewise inverse of the
-  // truncated two-sided tempered-stable jump measure.  mark_p = cm, cp, mu,
-  // alpha, eps, lda, y1, y2, y3, shift, eps^-alpha, -1/alpha.
-  static SDEMC_DI float inverse_cdf(const sdemc_inst& I, float y) {
-    const float cm = I.mark_p[0], cp = I.mark_p[1], mu = I.mark_p[2], al = I.mark_p[3];
-    const float lda = I.mark_p[5], y1 = I.mark_p[6], y2 = I.mark_p[7], y3 = I.mark_p[8];
-    const float epa = I.mark_p[10], nia = I.mark_p[11];
-    if (y <= y1) return logf((mu * lda * y) / cm) / mu - 1.0f;
-    if (y < y2) return -powf(al * ((lda * y / cm) - (1.0f / mu)) + 1.0f, nia);
-    if (y < y3)
-      return powf((-al / cp) * (lda * y - cm / mu - cm * ((epa - 1.0f) / al)) + epa, nia);
-    return 1.0f - (1.0f / mu) * logf(mu * lda * (1.0f - y) / cp);
-  }
-
+  // First jump time; fills the held and the reserve jump (all lanes together).
   SDEMC_DI float jump_first(const sdemc_inst& I) {
-    if (I.rate <= 0.f) { jmark = 0.f; jsel = 0; return __int_as_float(0x7f800000); }
-    jblock = 0;
-    return load_jump(I, 0);
+    cur_mark = 0.f; cur_sel = 0; res_gap = -1.f; res_mark = 0.f; res_sel = 0;
+    jblk = 0;
+    if (I.rate <= 0.f) return inf_f();
+    const JumpDraw j0 = jump_from_block<D>(I, ps.block(kTagJumps, 0));
+    const JumpDraw j1 = jump_from_block<D>(I, ps.block(kTagJumps, 1));
+    cur_mark = j0.mark; cur_sel = j0.sel;
+    res_gap = j1.gap; res_mark = j1.mark; res_sel = j1.sel;
+    jblk = 2;
+    return j0.gap;
   }
-  SDEMC_DI void jump_mark(int /*k*/, float& J, int& sel) const { J = jmark; sel = jsel; }
-  SDEMC_DI float jump_next(const sdemc_inst& I, float nj) {
-    ++jblock;
-    const float gap = load_jump(I, jblock);
+
+  // Divergent: the held jump fires now; returns the next jump time.  The
+  // reserve (res_gap >= 0) is promoted; a lane whose reserve is still empty
+  // draws its next block itself (rare: only between two batched refills).
+  SDEMC_DI float on_fire(const sdemc_inst& I, int /*k*/, float nj, float& J, int& sel) {
+    J = cur_mark;
+    sel = cur_sel;
+    float gap;
+    if (res_gap >= 0.f) {
+      gap = res_gap;
+      cur_mark = res_mark; cur_sel = res_sel;
+    } else {
+      const JumpDraw j = jump_from_block<D>(I, ps.block(kTagJumps, jblk));
+      ++jblk;
+      gap = j.gap;
+      cur_mark = j.mark; cur_sel = j.sel;
+    }
+    res_gap = -1.f;
     return __fadd_rn(nj, gap);
   }
-  SDEMC_DI int jumps_taken() const { return (int)jblock; }
+
+  // Warp-synchronous (all 32 lanes), every kRefillEvery-th step: when at
+  // least kRefillBatch live lanes have an empty reserve, refill them in one
+  // pass: worker w draws the block of the w-th requester and hands it back.
+  // `live` = the lane still steps (t < T) and may fire again.
+  SDEMC_DI void after_step(const sdemc_inst& I, int k, float& /*nj*/, bool live) {
+    if (I.rate <= 0.f || (k & (kRefillEvery - 1)) != kRefillEvery - 1) return;
+    const unsigned need = __ballot_sync(kFull, live && res_gap < 0.f);
+    const int nreq = __popc(need);
+    if (nreq < kRefillBatch) return;
+    const int lane = threadIdx.x & 31;
+    const int src = lane < nreq ? (int)__fns(need, 0, lane + 1) : lane;
+    const uint32_t c1 = __shfl_sync(kFull, ps.c1, src);
+    const uint32_t c2 = __shfl_sync(kFull, ps.c2base, src);
+    const uint32_t b = __shfl_sync(kFull, jblk, src);
+    const JumpDraw j = jump_from_block<D>(I, philox4x32_10(b, c1, c2 | (kTagJumps << 16), ps.c3, *ps.rk));
+    const int w = __popc(need & ((1u << lane) - 1u));
+    const float g = __shfl_sync(kFull, j.gap, w);
+    const float m = __shfl_sync(kFull, j.mark, w);
+    const int s = __shfl_sync(kFull, j.sel, w);
+    if (need & (1u << lane)) {
+      ++jblk;
+      res_gap = g; res_mark = m; res_sel = s;
+    }
+  }
 };
 
 // Replay draws: increments, marks and jump times recorded from the reference.
@@ -233,19 +312,19 @@ struct ReplayDraws {
   }
   SDEMC_DI float jump_first(const sdemc_inst& I) {
     jidx = 0;
-    if (I.rate <= 0.f || MJ <= 0) return __int_as_float(0x7f800000);
+    if (I.rate <= 0.f || MJ <= 0) return inf_f();
     return jt[0];
   }
-  SDEMC_DI void jump_mark(int k, float& J, int& sel) const {
+  // the reference draws a mark every step (sde_mc/solvers.py:211) and uses
+  // the one of the step where the jump fires
+  SDEMC_DI float on_fire(const sdemc_inst&, int k, float, float& J, int& sel) {
     J = (k < S) ? marks[k] : 0.f;
     sel = (asset != nullptr && k < S) ? asset[k] : 0;
-  }
-  SDEMC_DI float jump_next(const sdemc_inst&, float) {
     ++jidx;
-    if (jidx >= MJ) { overflow = true; return __int_as_float(0x7f800000); }
+    if (jidx >= MJ) { overflow = true; return inf_f(); }
     return jt[jidx];
   }
-  SDEMC_DI int jumps_taken() const { return jidx; }
+  SDEMC_DI void after_step(const sdemc_inst&, int, float&, bool) {}
 };
 
 // ------------------------------------------------------------- scheme -----
@@ -416,16 +495,24 @@ struct StoreSink {
   }
 };
 
+
 // ------------------------------------------------------------ the loop ----
+// Loop variants: kModeExact selects the reference's unfused Euler order;
+// kModeNominal keeps the state after num_steps steps for the payoff (what
+// mc_simple(payoff_time='terminal') reads from a jump solver's storage,
+// sde_mc/mc.py:84-86, 92).
+constexpr int kModeExact = 1;
+constexpr int kModeNominal = 2;
+
 // One path per lane; the warp steps in lock-step so that step k of every lane
 // draws from block k of its own stream (warp-uniform control, no divergence
 // on refills).  A lane whose t reached T is frozen (dt = 0, no jumps), which
 // is what the reference's batch-global loop does to finished paths
 // (sde_mc/solvers.py:182, 190-191).  Returns the number of active steps.
-template <int D, int NOISE, bool EXACT, class Draws, class Sink>
-SDEMC_DI int simulate(const sdemc_inst& I, Draws& dr, Sink& sk, float* x,
-                      int max_iters, bool& overflow) {
+template <int D, int NOISE, int MODE, class Draws, class Sink>
+SDEMC_DI int simulate(const sdemc_inst& I, Draws& dr, Sink& sk, float* x, int max_iters, bool& overflow) {
   using L = Layout<D, NOISE>;
+  constexpr bool EXACT = (MODE & kModeExact) != 0;
 #pragma unroll
   for (int i = 0; i < D; ++i) x[i] = I.x0[i];
   sk.template init<D>(x);
@@ -452,12 +539,11 @@ SDEMC_DI int simulate(const sdemc_inst& I, Draws& dr, Sink& sk, float* x,
   float nj = dr.jump_first(I);
   int own = 0;
   bool act = t < T;
-  // mc_simple(payoff_time='terminal') on a jump solver reads column num_steps
-  // of the storage (sde_mc/mc.py:84-86, 92): keep that state when asked.
-  const bool at_nominal = (I.flags & SDEMC_INST_PAYOFF_AT_NOMINAL_STEP) != 0;
-  float xcap[D];
+  float xcap[(MODE & kModeNominal) ? D : 1];
+  if (MODE & kModeNominal) {
 #pragma unroll
-  for (int i = 0; i < D; ++i) xcap[i] = x[i];
+    for (int i = 0; i < D; ++i) xcap[i] = x[i];
+  }
   while (__any_sync(kFull, act)) {
     if (k >= max_iters) { overflow = true; break; }
     // h = min(h, max(T - t, 0)); dt = min(h, next_jump - t)
@@ -478,23 +564,27 @@ SDEMC_DI int simulate(const sdemc_inst& I, Draws& dr, Sink& sk, float* x,
     float J = 0.f;
     int sel = 0;
     if (act && jump_due(nj, t)) {
-      dr.jump_mark(k, J, sel);
+      nj = dr.on_fire(I, k, nj, J, sel);
       apply_jump<D, EXACT>(I, x, I.exact_jumps ? x : old, J, sel);
-      nj = dr.jump_next(I, nj);
     }
     sk.template step<D, L::NW>(k, Sink::kWantsLeft ? xl : x, x, t, J, sel, dW, dW2, z, jump_one);
     own += act ? 1 : 0;
-    if (at_nominal && act && own == I.num_steps) {
+    if (MODE & kModeNominal) {
+      if (act && own == I.num_steps) {
 #pragma unroll
-      for (int i = 0; i < D; ++i) xcap[i] = x[i];
+        for (int i = 0; i < D; ++i) xcap[i] = x[i];
+      }
     }
     ++k;
     act = t < T;
+    dr.after_step(I, k, nj, act);
   }
   sk.template finish<D, L::NW>(k, x, t);
-  if (at_nominal && own >= I.num_steps) {
+  if (MODE & kModeNominal) {
+    if (own >= I.num_steps) {
 #pragma unroll
-    for (int i = 0; i < D; ++i) x[i] = xcap[i];
+      for (int i = 0; i < D; ++i) x[i] = xcap[i];
+    }
   }
   return own;
 }

@@ -24,15 +24,27 @@ int validate_inst(const sdemc_inst* I);
 int max_iterations(const sdemc_inst* I);
 
 constexpr int kChunk = SDEMC_CHUNK_PATHS;
-constexpr size_t kScratchHeader = 256;   // status word + padding
+constexpr int kGroup = 256;              // chunks per first-level reduction group
+constexpr size_t kScratchHeader = 256;   // status word, completion counter, padding
 
 inline int64_t num_chunks(const sdemc_inst* I) {
   return (I->num_paths + kChunk - 1) / kChunk;
 }
 
-// Launch the deterministic FP64 chunk reduction (K10).
-int launch_reduce(const double* part, int64_t nchunks, int width, int32_t* status,
-                  double* out, cudaStream_t s);
+// Scratch layout: [header][nchunks x width doubles][ngroups x width doubles].
+constexpr int64_t num_groups_for(int64_t nchunks) {
+  return nchunks > 0 ? (nchunks + kGroup - 1) / kGroup : 1;
+}
+constexpr size_t scratch_bytes_for(int64_t nchunks, int width) {
+  return kScratchHeader + (size_t)(nchunks + num_groups_for(nchunks)) * width * sizeof(double);
+}
+inline int32_t* scratch_status(void* s) { return (int32_t*)s; }
+inline unsigned* scratch_counter(void* s) { return (unsigned*)((char*)s + 4); }
+inline double* scratch_chunks(void* s) { return (double*)((char*)s + kScratchHeader); }
+
+// Launch the deterministic FP64 chunk reduction (K10) over the chunk partials
+// in `scratch`; writes sums, mean, var and the status word to out.
+int launch_reduce(void* scratch, int64_t nchunks, int width, double* out, cudaStream_t s);
 
 }  // namespace sdemc
 

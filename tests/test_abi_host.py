@@ -41,9 +41,10 @@ def test_scratch_sizes():
     import ctypes
     inst = inst_for(merton1d(), num_paths=1000)
     lib = N.load()
-    nch = (1000 + 127) // 128
-    assert lib.sdemc_price_scratch_bytes(ctypes.byref(inst)) == 256 + nch * 3 * 8
-    assert lib.sdemc_mlmc_scratch_bytes(ctypes.byref(inst)) == 256 + nch * 5 * 8
+    nch = (1000 + 31) // 32          # chunks of one warp round
+    ngroups = (nch + 255) // 256     # first-level reduction groups
+    assert lib.sdemc_price_scratch_bytes(ctypes.byref(inst)) == 256 + (nch + ngroups) * 3 * 8
+    assert lib.sdemc_mlmc_scratch_bytes(ctypes.byref(inst)) == 256 + (nch + ngroups) * 5 * 8
 
 
 def test_lowering_uses_reference_float32_coefficients(kat):

@@ -50,7 +50,7 @@ def test_noalloc_matches_price_on_two_calls_in_a_row():
 def test_noalloc_rejects_sizes_over_the_limit():
     N.require_cuda()
     lib = N.load()
-    assert lib.sdemc_price_noalloc_scratch_bytes() >= 256 + (1 << 23) // 128 * 24
+    assert lib.sdemc_price_noalloc_scratch_bytes() >= 256 + (1 << 23) // 32 * 24
     inst = inst_for(merton1d(10), num_paths=(1 << 23) + 1, seed=1)
     out = torch.zeros(6, dtype=torch.float64, device="cuda")
     rc = lib.sdemc_price_noalloc(ctypes.byref(inst), None, N.ptr(out), None, N.stream_handle(out.device))
