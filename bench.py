@@ -204,6 +204,70 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+MIX_WORKLOAD = ("config-3 mix: 512 correlated Merton basket calls, d~U{1..8}, steps log-U[32,512], "
+                "paths log-U[2^12,2^18], K~U(0.8,1.2), sigma_i~U(0.1,0.4), rate~U(0.5,3), rho 0.3, "
+                "logN(-0.1,0.2) jumps; numpy default_rng(0)")
+
+
+def bench_batched_mix(steps, warmup):
+    """Config 3: the whole mix per step, batched (K8, autotuned, CUDA graph)
+    against the plain method one request per launch (K1 + K10 each)."""
+    import torch
+    from sde_mc_gb300 import batch as B
+    from sde_mc_gb300 import kernels as K
+    from sde_mc_gb300 import workloads
+    mix = workloads.basket_mix(512)
+    n = len(mix)
+    offs = [0] * n
+    insts = B.lower_mix(mix, offs)
+    plan = B.BatchPlan(insts)
+    tune = B.autotune(plan, repeats=2)
+    steps = max(1, min(steps, 10))
+    plan.set_path_offsets([(1 << 40) + m.paths * 0 for m in mix])
+    plan.run()
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        plan.upload()
+        plan.launch()
+    ms = []
+    for s in range(warmup + steps):
+        plan.set_path_offsets([(s + 2) * (1 << 24) for _ in mix])
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        graph.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        if s >= warmup:
+            ms.append(e0.elapsed_time(e1))
+    rows = plan.out[:n].cpu().numpy()
+    batched_ms = sum(ms) / len(ms)
+    # plain: one request per launch, descriptors lowered ahead of time
+    plain_insts = B.lower_mix(mix, [(1 << 41)] * n)
+    outs = [torch.empty(6, dtype=torch.float64, device="cuda") for _ in range(n)]
+    pm = []
+    for s in range(max(1, warmup // 2) + steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for ins, o in zip(plain_insts, outs):
+            K.price(ins, out=o)
+        e1.record()
+        torch.cuda.synchronize()
+        if s >= max(1, warmup // 2):
+            pm.append(e0.elapsed_time(e1))
+    plain_ms = sum(pm) / len(pm)
+    work = sum(m.paths * (m.solver.num_steps + float(m.solver.sde.jump_rate())) for m in mix)
+    return {"workload": MIX_WORKLOAD, "instances": n, "steps": steps,
+            "batched": {"prices_per_s": n / (batched_ms * 1e-3), "ms_per_mix": batched_ms,
+                        "launch": {"block_threads": tune["choice"][0], "side_streams": tune["choice"][1]},
+                        "graph": True, "gpu_launches_per_mix": 1 + 1 + len(plan.classes[:plan.header.n_class])},
+            "plain_one_per_launch": {"prices_per_s": n / (plain_ms * 1e-3), "ms_per_mix": plain_ms,
+                                     "gpu_launches_per_mix": 2 * n},
+            "speedup_batched_vs_plain": plain_ms / batched_ms,
+            "path_steps_per_mix": work, "batched_path_steps_per_s": work / (batched_ms * 1e-3),
+            "status_ok": bool((rows[:, 5] == 0).all())}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -342,6 +406,7 @@ def main():
     }
     if rank == 0:
         line["clocks"] = clk.summary()
+        line["batched_mix"] = bench_batched_mix(args.steps, args.warmup)
         from sde_mc_gb300.lowering import lower as lw
 
         def factory(n):

@@ -208,6 +208,44 @@ size_t sdemc_price_noalloc_scratch_bytes(void);
 int sdemc_price_noalloc(const sdemc_inst* h_inst, const sdemc_cfg* h_cfg,
                         double* d_out, float* d_payoffs, void* stream);
 
+/* ---- K8: batched heterogeneous pricing --------------------------------
+ * No single reference counterpart: it prices many instances (different dim,
+ * steps, paths, payoffs) in one pass, each exactly as sdemc_price would
+ * alone (bit-identical results), i.e. a loop of mc_simple calls
+ * (sde_mc/mc.py:53-123) over run_mc requests (sde_mc/mc.py:437-440).
+ *
+ * sdemc_batch_plan (host only) groups the instances into classes of equal
+ * (dim, noise layout, loop variant), orders each class by descending cost and
+ * writes a self-contained plan blob of sdemc_batch_plan_bytes(n) bytes into
+ * h_blob.  The caller copies the blob to device memory (d_blob) and calls
+ * sdemc_price_batch, which launches one persistent kernel per class (warps
+ * take 32-path chunks from a per-class counter) and one FP64 reduction for
+ * all instances.  d_out receives n rows of (sum, sum_sq, n, mean, var,
+ * status) in the caller's instance order.  d_scratch (size
+ * sdemc_batch_scratch_bytes(h_blob)) must be zeroed before its first use.
+ * h_cfgs (nullable) holds one launch configuration per class in class order;
+ * side_streams (nullable, n_side entries) lets class kernels overlap; the
+ * calls on them are joined back into `stream` before the reduction.         */
+typedef struct sdemc_batch_class {
+  int32_t dim, noise, mode, count;  /* mode: bit 0 exact Euler, bit 1 nominal */
+  int32_t first;                    /* first instance (plan order)            */
+  int32_t reserved;
+  int64_t chunk_begin, chunk_end;   /* global chunk range of the class        */
+} sdemc_batch_class;
+
+typedef struct sdemc_batch_header {
+  int32_t n_inst, n_class;
+  int64_t total_chunks, total_groups;
+  int64_t off_classes, off_insts, off_order, off_chunk_prefix, off_group_prefix;
+} sdemc_batch_header;
+
+size_t sdemc_batch_plan_bytes(int n);
+int sdemc_batch_plan(const sdemc_inst* h_insts, int n, void* h_blob, size_t blob_bytes);
+size_t sdemc_batch_scratch_bytes(const void* h_blob);
+int sdemc_price_batch(const void* h_blob, const void* d_blob, void* d_scratch,
+                      size_t scratch_bytes, double* d_out, const sdemc_cfg* h_cfgs,
+                      void* const* side_streams, int n_side, void* stream);
+
 /* ---- K3: replay of recorded draws --------------------------------------
  * Runs the reference's jump-adapted loop (sde_mc/solvers.py:164-226, or its
  * uniform-grid twin :68-88) on draws exported from the reference: d_jump_times

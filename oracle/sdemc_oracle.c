@@ -105,10 +105,14 @@ static float inverse_cdf(const sdemc_inst* I, float y) {
   const float cm = I->mark_p[0], cp = I->mark_p[1], mu = I->mark_p[2], al = I->mark_p[3];
   const float lda = I->mark_p[5], y1 = I->mark_p[6], y2 = I->mark_p[7], y3 = I->mark_p[8];
   const float epa = I->mark_p[10], nia = I->mark_p[11];
-  if (y <= y1) return logf((mu * lda * y) / cm) / mu - 1.0f;
-  if (y < y2) return -powf(al * ((lda * y / cm) - (1.0f / mu)) + 1.0f, nia);
-  if (y < y3) return powf((-al / cp) * (lda * y - cm / mu - cm * ((epa - 1.0f) / al)) + epa, nia);
-  return 1.0f - (1.0f / mu) * logf(mu * lda * (1.0f - y) / cp);
+  const float ly = lda * y, inv_mu = 1.0f / mu;
+  if (y <= y1) return logf((mu * ly) / cm) / mu - 1.0f;
+  if (y < y2) return -powf(al * (ly / cm - inv_mu) + 1.0f, nia);
+  if (y < y3) {
+    const float tail = cm * ((epa - 1.0f) / al);
+    return powf((-al / cp) * ((ly - cm / mu) - tail) + epa, nia);
+  }
+  return 1.0f - inv_mu * logf(((mu * lda) * (1.0f - y)) / cp);
 }
 
 static float native_load_jump(const sdemc_inst* I, int D, draws_t* d, uint32_t j) {

@@ -76,6 +76,10 @@ _PROTOS = {
     "sdemc_price": (_I, [_P, _P, _P, ctypes.c_size_t, _P, _P, _P]),
     "sdemc_price_chunks": (_I, [_P, _P, _P, ctypes.c_size_t, _P, _P]),
     "sdemc_reduce_chunks": (_I, [_P, ctypes.c_int64, _I, _P, _P]),
+    "sdemc_batch_plan_bytes": (ctypes.c_size_t, [_I]),
+    "sdemc_batch_plan": (_I, [_P, _I, _P, ctypes.c_size_t]),
+    "sdemc_batch_scratch_bytes": (ctypes.c_size_t, [_P]),
+    "sdemc_price_batch": (_I, [_P, _P, _P, ctypes.c_size_t, _P, _P, _P, _I, _P]),
     "sdemc_price_noalloc_scratch_bytes": (ctypes.c_size_t, []),
     "sdemc_price_noalloc": (_I, [_P, _P, _P, _P, _P]),
     "sdemc_replay": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),

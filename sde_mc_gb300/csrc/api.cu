@@ -59,13 +59,7 @@ int validate_inst(const sdemc_inst* I) {
   return SDEMC_OK;
 }
 
-int max_iterations(const sdemc_inst* I) {
-  if (I->grid == SDEMC_GRID_UNIFORM) return I->num_steps;
-  const double lam = (double)I->rate * (double)I->T;
-  const double tail = lam + 12.0 * sqrt(lam > 1.0 ? lam : 1.0) + 64.0;
-  const double cap = (double)I->num_steps + 2.0 * tail + 8.0;
-  return cap > 2.0e9 ? 2000000000 : (int)cap;
-}
+int max_iterations(const sdemc_inst* I) { return max_iterations_hd(*I); }
 
 // ----------------------------------------------------------------- K10 -----
 // Two fixed levels in one launch.  CTA g sums chunks [256g, 256g + 256) with a
@@ -143,8 +137,8 @@ __global__ void philox_kernel(uint64_t seed, uint32_t stream_id, uint32_t tag, u
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const RoundKeys rk = make_round_keys(seed);
-  PathStream k;
-  k.init(&rk, stream_id, path);
+  PathStream<ConstKeys> k;
+  k.init(ConstKeys{&rk}, stream_id, path);
   const U4 w = k.block(tag, first + (uint32_t)i);
   out[4 * i + 0] = w.x; out[4 * i + 1] = w.y; out[4 * i + 2] = w.z; out[4 * i + 3] = w.w;
 }

@@ -101,7 +101,7 @@ mlmc_kernel(const __grid_constant__ LevelParams P, int factor, float hf, float h
   for (int64_t c = warp; c < nchunks; c += nwarps) {
     const int64_t p = c * kChunk + lane;
     NativeDraws<D, NOISE> dr;
-    dr.init(I, (uint64_t)p, &P.rk);
+    dr.init(I, (uint64_t)p, ConstKeys{&P.rk});
     float xf[D], xc[D];
     simulate_pair<D, NOISE, false>(I, dr, factor, hf, hc, xf, xc, max_iters, ovf);
     const bool valid = p < I.num_paths;
@@ -153,7 +153,7 @@ mlmc_terminals_kernel(const __grid_constant__ LevelParams P, int factor, float h
   const sdemc_inst& I = P.I;
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   NativeDraws<D, NOISE> dr;
-  dr.init(I, (uint64_t)p, &P.rk);
+  dr.init(I, (uint64_t)p, ConstKeys{&P.rk});
   bool ovf = false;
   float xf[D], xc[D];
   simulate_pair<D, NOISE, false>(I, dr, factor, hf, hc, xf, xc, max_iters, ovf);

@@ -33,7 +33,7 @@ price_kernel(const __grid_constant__ PriceParams P, double* __restrict__ part,
   for (int64_t c = warp; c < nchunks; c += nwarps) {
     const int64_t p = c * kChunk + lane;
     NativeDraws<D, NOISE> dr;
-    dr.init(I, (uint64_t)p, &P.rk);
+    dr.init(I, (uint64_t)p, ConstKeys{&P.rk});
     NullSink sk;
     float x[D];
     simulate<D, NOISE, MODE>(I, dr, sk, x, max_iters, ovf);

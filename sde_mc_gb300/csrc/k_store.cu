@@ -39,7 +39,7 @@ materialise_kernel(const __grid_constant__ StoreParams P, int S, float* paths, f
     sk.z = zout ? zout + (size_t)p * S * zdim : nullptr;
   }
   NativeDraws<D, NOISE> dr;
-  dr.init(I, (uint64_t)p, &P.rk);
+  dr.init(I, (uint64_t)p, ConstKeys{&P.rk});
   bool ovf = false;
   float x[D];
   const int it = max_iters < S ? max_iters : S;

@@ -39,12 +39,28 @@ SDEMC_HDI RoundKeys make_round_keys(uint64_t seed) {
   return rk;
 }
 
-SDEMC_DI U4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, const RoundKeys& rk) {
+// Key sources: the round keys as launch constants (single-instance kernels,
+// where they become constant-bank operands), or the seed in two registers
+// with the key schedule folded into each round (kernels whose instance
+// changes per chunk and would otherwise hold twenty keys in registers).
+struct SeedKeys {
+  uint32_t k0, k1;
+  SDEMC_DI uint32_t a(int r) const { return k0 + (uint32_t)r * 0x9E3779B9u; }
+  SDEMC_DI uint32_t b(int r) const { return k1 + (uint32_t)r * 0xBB67AE85u; }
+};
+struct ConstKeys {
+  const RoundKeys* rk;
+  SDEMC_DI uint32_t a(int r) const { return rk->k[2 * r]; }
+  SDEMC_DI uint32_t b(int r) const { return rk->k[2 * r + 1]; }
+};
+
+template <class KS>
+SDEMC_DI U4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, const KS& ks) {
 #pragma unroll
   for (int r = 0; r < 10; ++r) {
     const uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
     const uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
-    const uint32_t n0 = hi1 ^ c1 ^ rk.k[2 * r], n2 = hi0 ^ c3 ^ rk.k[2 * r + 1];
+    const uint32_t n0 = hi1 ^ c1 ^ ks.a(r), n2 = hi0 ^ c3 ^ ks.b(r);
     c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
   }
   return U4{c0, c1, c2, c3};
@@ -68,17 +84,18 @@ constexpr uint32_t kTagJumps = 1u;
 
 // Counter words of one path: c1 = path low word, c2 = path high 16 bits |
 // tag << 16, c3 = stream id; c0 is the block index.
+template <class KS>
 struct PathStream {
-  const RoundKeys* rk;
+  KS ks;
   uint32_t c1, c2base, c3;
-  SDEMC_DI void init(const RoundKeys* keys, uint32_t stream_id, uint64_t gpath) {
-    rk = keys;
+  SDEMC_DI void init(const KS& keys, uint32_t stream_id, uint64_t gpath) {
+    ks = keys;
     c1 = (uint32_t)gpath;
     c2base = (uint32_t)(gpath >> 32) & 0xFFFFu;
     c3 = stream_id;
   }
   SDEMC_DI U4 block(uint32_t tag, uint32_t b) const {
-    return philox4x32_10(b, c1, c2base | (tag << 16), c3, *rk);
+    return philox4x32_10(b, c1, c2base | (tag << 16), c3, ks);
   }
 };
 
@@ -113,14 +130,25 @@ SDEMC_DI void correlate(const sdemc_inst& I, const float* z, float sq, float* dW
 // InverseCdf.__call__ (sde_mc/levy.py:22-30): piecewise inverse of the
 // truncated two-sided tempered-stable jump measure.  mark_p = cm, cp, mu,
 // alpha, eps, lda, y1, y2, y3, shift, eps^-alpha, -1/alpha.
+// Every operation is an explicit _rn intrinsic so that no kernel's inlining
+// context can change a rounding (results must not depend on the kernel).
 SDEMC_DI float inverse_cdf(const sdemc_inst& I, float y) {
   const float cm = I.mark_p[0], cp = I.mark_p[1], mu = I.mark_p[2], al = I.mark_p[3];
   const float lda = I.mark_p[5], y1 = I.mark_p[6], y2 = I.mark_p[7], y3 = I.mark_p[8];
   const float epa = I.mark_p[10], nia = I.mark_p[11];
-  if (y <= y1) return logf((mu * lda * y) / cm) / mu - 1.0f;
-  if (y < y2) return -powf(al * ((lda * y / cm) - (1.0f / mu)) + 1.0f, nia);
-  if (y < y3) return powf((-al / cp) * (lda * y - cm / mu - cm * ((epa - 1.0f) / al)) + epa, nia);
-  return 1.0f - (1.0f / mu) * logf(mu * lda * (1.0f - y) / cp);
+  const float ly = __fmul_rn(lda, y);
+  const float inv_mu = __fdiv_rn(1.0f, mu);
+  if (y <= y1)
+    return __fsub_rn(__fdiv_rn(logf(__fdiv_rn(__fmul_rn(mu, ly), cm)), mu), 1.0f);
+  if (y < y2)
+    return -powf(__fadd_rn(__fmul_rn(al, __fsub_rn(__fdiv_rn(ly, cm), inv_mu)), 1.0f), nia);
+  if (y < y3) {
+    const float tail = __fmul_rn(cm, __fdiv_rn(__fsub_rn(epa, 1.0f), al));
+    const float arg = __fsub_rn(__fsub_rn(ly, __fdiv_rn(cm, mu)), tail);
+    return powf(__fadd_rn(__fmul_rn(__fdiv_rn(-al, cp), arg), epa), nia);
+  }
+  const float q = __fdiv_rn(__fmul_rn(__fmul_rn(mu, lda), __fsub_rn(1.0f, y)), cp);
+  return __fsub_rn(1.0f, __fmul_rn(inv_mu, logf(q)));
 }
 
 // One jump-stream block: x -> exponential gap, y (,z) -> lognormal mark (Box-
@@ -130,12 +158,12 @@ struct JumpDraw { float gap, mark; int sel; };
 template <int D>
 SDEMC_DI JumpDraw jump_from_block(const sdemc_inst& I, U4 w) {
   JumpDraw j;
-  j.gap = -logf(u01(w.x)) * I.inv_rate;
+  j.gap = __fmul_rn(-logf(u01(w.x)), I.inv_rate);
   if (I.mark == SDEMC_MARK_LOGNORMAL) {
-    const float zn = bm_radius(w.y) * __cosf(bm_angle(w.z));
-    j.mark = expf(I.mark_p[1] * zn + I.mark_p[0]) - 1.0f;
+    const float zn = __fmul_rn(bm_radius(w.y), __cosf(bm_angle(w.z)));
+    j.mark = __fsub_rn(expf(__fmaf_rn(I.mark_p[1], zn, I.mark_p[0])), 1.0f);
   } else if (I.mark == SDEMC_MARK_INVCDF) {
-    j.mark = inverse_cdf(I, u01(w.y) + I.mark_p[9]);
+    j.mark = inverse_cdf(I, __fadd_rn(u01(w.y), I.mark_p[9]));
   } else {
     j.mark = 0.f;
   }
@@ -149,6 +177,18 @@ SDEMC_DI JumpDraw jump_from_block(const sdemc_inst& I, U4 w) {
 }
 
 SDEMC_DI float inf_f() { return __int_as_float(0x7f800000); }
+
+// Iteration cap of the adapted loop: nominal steps plus a Poisson tail bound
+// on the jump count, plus room for end-of-interval steps.  A path that needs
+// more is reported as SDEMC_EOVERFLOW (the reference raises IndexError when
+// it runs out of pre-drawn jump times, sde_mc/solvers.py:133, 187).
+SDEMC_HDI int max_iterations_hd(const sdemc_inst& I) {
+  if (I.grid == SDEMC_GRID_UNIFORM) return I.num_steps;
+  const double lam = (double)I.rate * (double)I.T;
+  const double tail = lam + 12.0 * sqrt(lam > 1.0 ? lam : 1.0) + 64.0;
+  const double cap = (double)I.num_steps + 2.0 * tail + 8.0;
+  return cap > 2.0e9 ? 2000000000 : (int)cap;
+}
 
 // ------------------------------------------------------------- draws -------
 // Native draws: counter-based Philox streams of one path.
@@ -164,18 +204,18 @@ SDEMC_DI float inf_f() { return __int_as_float(0x7f800000); }
 constexpr int kRefillBatch = 8;
 constexpr int kRefillEvery = 4;
 
-template <int D, int NOISE>
+template <int D, int NOISE, class KS = ConstKeys>
 struct NativeDraws {
   using L = Layout<D, NOISE>;
-  PathStream ps;
+  PathStream<KS> ps;
   float buf[4];          // buffered normals when ZD in {1,2}
   float sq_h, h_nom;     // cached sqrt of the nominal step
   float cur_mark, res_gap, res_mark;
   uint32_t jblk;         // next jump-stream block to draw
   int cur_sel, res_sel;
 
-  SDEMC_DI void init(const sdemc_inst& I, uint64_t gpath, const RoundKeys* rk) {
-    ps.init(rk, I.stream_id, I.path_offset + gpath);
+  SDEMC_DI void init(const sdemc_inst& I, uint64_t gpath, const KS& ks) {
+    ps.init(ks, I.stream_id, I.path_offset + gpath);
     h_nom = I.h;
     sq_h = sqrtf(I.h);
   }
@@ -273,7 +313,7 @@ struct NativeDraws {
     const uint32_t c1 = __shfl_sync(kFull, ps.c1, src);
     const uint32_t c2 = __shfl_sync(kFull, ps.c2base, src);
     const uint32_t b = __shfl_sync(kFull, jblk, src);
-    const JumpDraw j = jump_from_block<D>(I, philox4x32_10(b, c1, c2 | (kTagJumps << 16), ps.c3, *ps.rk));
+    const JumpDraw j = jump_from_block<D>(I, philox4x32_10(b, c1, c2 | (kTagJumps << 16), ps.c3, ps.ks));
     const int w = __popc(need & ((1u << lane) - 1u));
     const float g = __shfl_sync(kFull, j.gap, w);
     const float m = __shfl_sync(kFull, j.mark, w);

@@ -17,10 +17,7 @@ int num_sms();
 // Validate the parts of a descriptor every kernel relies on.
 int validate_inst(const sdemc_inst* I);
 
-// Iteration cap of the adapted loop: nominal steps plus a Poisson tail bound
-// on the jump count, plus room for end-of-interval steps.  A path that needs
-// more is reported as SDEMC_EOVERFLOW (the reference raises IndexError when
-// it runs out of pre-drawn jump times, sde_mc/solvers.py:133, 187).
+// Iteration cap of the adapted loop (max_iterations_hd in sdemc_device.cuh).
 int max_iterations(const sdemc_inst* I);
 
 constexpr int kChunk = SDEMC_CHUNK_PATHS;

@@ -166,3 +166,58 @@ def test_no_cpu_fallback():
         sm.mc_simple(1000, solver, payoff, disc, bs=1000)
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         solver.solve(8)
+
+
+def test_batch_plan_groups_and_orders():
+    """The host planner (no GPU needed): classes of equal (dim, noise, mode),
+    contiguous chunk runs, descending cost inside a class, a permutation back
+    to the caller's order, chunk/group prefix sums."""
+    import ctypes
+    from sde_mc_gb300 import batch as B
+    from sde_mc_gb300 import workloads
+    mix = workloads.basket_mix(64, device="cpu")
+    insts = B.lower_mix(mix)
+    n = len(insts)
+    lib = N.load()
+    nbytes = lib.sdemc_batch_plan_bytes(n)
+    buf = ctypes.create_string_buffer(nbytes)
+    arr = (N.SdemcInst * n)(*insts)
+    assert lib.sdemc_batch_plan(ctypes.cast(arr, ctypes.c_void_p), n, buf, nbytes) == 0
+    base = ctypes.addressof(buf)
+    H = B.BatchHeader.from_address(base)
+    assert H.n_inst == n
+    classes = (B.BatchClass * H.n_class).from_address(base + H.off_classes)
+    order = list((ctypes.c_int32 * n).from_address(base + H.off_order))
+    cp = list((ctypes.c_int64 * (n + 1)).from_address(base + H.off_chunk_prefix))
+    gp = list((ctypes.c_int64 * (n + 1)).from_address(base + H.off_group_prefix))
+    plan = (N.SdemcInst * n).from_address(base + H.off_insts)
+    assert sorted(order) == list(range(n))
+    keys = set()
+    for c in classes:
+        assert (c.dim, c.noise, c.mode) not in keys
+        keys.add((c.dim, c.noise, c.mode))
+        costs = [plan[j].num_steps + plan[j].rate for j in range(c.first, c.first + c.count)]
+        assert costs == sorted(costs, reverse=True)
+        assert all(plan[j].dim == c.dim for j in range(c.first, c.first + c.count))
+        assert c.chunk_begin == cp[c.first] and c.chunk_end == cp[c.first + c.count]
+    assert sum(c.count for c in classes) == n
+    for j in range(n):
+        assert plan[j].num_paths == insts[order[j]].num_paths
+        assert cp[j + 1] - cp[j] == (insts[order[j]].num_paths + 31) // 32
+        assert gp[j + 1] - gp[j] == max(1, (cp[j + 1] - cp[j] + 255) // 256)
+    assert H.total_chunks == cp[n] and H.total_groups == gp[n]
+    assert lib.sdemc_batch_plan(ctypes.cast(arr, ctypes.c_void_p), n, buf, nbytes - 1) == N.ENOMEM
+
+
+def test_basket_mix_law():
+    """Config-3 instance distribution: ranges and the stated draw order."""
+    from sde_mc_gb300 import workloads
+    mix = workloads.basket_mix(512, device="cpu")
+    dims = [m.dim for m in mix]
+    steps = [m.solver.num_steps for m in mix]
+    paths = [m.paths for m in mix]
+    assert set(dims) == set(range(1, 9))
+    assert 32 <= min(steps) and max(steps) <= 512
+    assert 2 ** 12 <= min(paths) and max(paths) <= 2 ** 18
+    assert all(0.8 <= m.payoff.strike <= 1.2 for m in mix)
+    assert [m.stream_id for m in mix] == list(range(512))
