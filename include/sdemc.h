@@ -306,6 +306,39 @@ int sdemc_mlmc_replay(const sdemc_inst* h_inst, int fine, int coarse,
                       const int32_t* d_asset, float* d_xf, float* d_xc,
                       int32_t* d_status, void* stream);
 
+/* ---- K5/K6: learned control variate -------------------------------------
+ * The integrand network of the adapted control variate, the reference's
+ * Mlp(1+d, [64, 64, 64], d) with ReLU and no batch norm (sde_mc/nets.py:39-93),
+ * for d in {1, 2}.  Parameters: one FP32 vector of sdemc_cv_nparams(d) values
+ * in torch's order (W1 (64, 1+d), b1, W2, b2, W3, b3, W4 (d, 64), b4).
+ * Data: the AdaptedPathData tensors of a materialised run (d_time (N, S+1),
+ * d_paths (N, S+1, d), d_normals (N, S, d), discounted d_payoffs (N)); the
+ * last column is dropped as sde_mc/nets.py:194-199 does.  d_index (nullable,
+ * n entries) selects and orders the paths (a shuffled minibatch).
+ *
+ * sdemc_cv_forward: d_gamma[q] = payoff + sum_k e^{-r t_k} f(t_k, X_k) . dW_k
+ * for path index[q] (apply_adapted_control_variates with g = 0,
+ * sde_mc/varred.py:98-131, integrate_cv :202-214); d_fout (nullable, (N, S, d))
+ * receives f.  Hidden 64x64 layers on BF16 tensor cores, FP32 accumulation.
+ * sdemc_cv_backward: gradient of Var(Gamma) over the n selected paths
+ * (sde_mc/varred.py:160-180) into d_grad, using d_gamma from a forward call on
+ * the same selection; d_partials holds nparts x nparams floats.
+ * sdemc_adam_step: one torch.optim.Adam step (no weight decay).             */
+int sdemc_cv_nparams(int dim);
+int sdemc_cv_forward(int dim, const float* d_params, const float* d_time,
+                     const float* d_paths, const float* d_normals,
+                     const float* d_payoffs, const int64_t* d_index, int64_t n,
+                     int steps, float disc_rate, float* d_gamma, float* d_fout,
+                     void* stream);
+int sdemc_cv_backward(int dim, const float* d_params, const float* d_time,
+                      const float* d_paths, const float* d_normals,
+                      const int64_t* d_index, int64_t n, int steps,
+                      float disc_rate, const float* d_gamma, float* d_partials,
+                      int nparts, float* d_grad, void* stream);
+int sdemc_adam_step(float* d_params, const float* d_grad, float* d_m, float* d_v,
+                    int nparam, int step, float lr, float beta1, float beta2,
+                    float eps, void* stream);
+
 /* ---- RNG export (for the oracle and for users who want the raw draws) --
  * Philox4x32-10 blocks for counter (c0 = first_block + i, c1 = path lo,
  * c2 = path hi | tag << 16, c3 = stream_id), key = seed.                   */

@@ -270,3 +270,75 @@ def adam_step(params, grads, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8, state=None, st
         new.append(p - lr * mh / (np.sqrt(vh) + eps))
         st.append((m, v))
     return new, st
+
+
+# ----------------------------------------- mixed-precision restatement ----
+# The GPU network kernels keep layer 1 and layer 4 in FP32 and run the two
+# 64x64 layers on BF16 tensor cores with FP32 accumulation.  These functions
+# restate that precision policy in numpy (BF16 roundings where the kernels
+# round, FP64 sums elsewhere), so that kernel bugs separate from rounding: the
+# GPU agrees with them to FP32 accumulation-order noise, and they agree with
+# the FP32 reference network (mlp_forward / cv_loss_and_grads) to BF16 noise.
+def bf16_round(x):
+    """float32 -> nearest bfloat16 (ties to even), returned as float32."""
+    a = np.ascontiguousarray(x, dtype=np.float32)
+    u = a.view(np.uint32).astype(np.uint64)
+    u = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return u.astype(np.uint32).view(np.float32).reshape(a.shape)
+
+
+def _f32(x):
+    return np.asarray(x, dtype=np.float64).astype(np.float32).astype(np.float64)
+
+
+def mlp_forward_mixed(params, t, x):
+    """Kernel-precision forward.  t (R,), x (R, d); params as mlp_forward.
+    Returns (out, cache) with the BF16 activations the backward needs."""
+    W1, b1, W2, b2, W3, b3, W4, b4 = [np.asarray(p, dtype=np.float32) for p in params]
+    t = np.asarray(t, dtype=np.float32).astype(np.float64)
+    x = np.asarray(x, dtype=np.float32).astype(np.float64)
+    z = _f32(W1[:, 0].astype(np.float64)[None, :] * t[:, None] + b1.astype(np.float64)[None, :])
+    for i in range(x.shape[1]):
+        z = _f32(W1[:, 1 + i].astype(np.float64)[None, :] * x[:, i:i + 1] + z)
+    h1b = bf16_round(np.maximum(z, 0.0)).astype(np.float64)
+    w2b = bf16_round(W2).astype(np.float64)
+    w3b = bf16_round(W3).astype(np.float64)
+    z2 = _f32(h1b @ w2b.T + b2.astype(np.float64))
+    h2b = bf16_round(np.maximum(z2, 0.0)).astype(np.float64)
+    z3 = _f32(h2b @ w3b.T + b3.astype(np.float64))
+    h3 = np.maximum(z3, 0.0)
+    out = _f32(h3 @ W4.astype(np.float64).T + b4.astype(np.float64))
+    return out, dict(h1b=h1b, h2b=h2b, h3=h3, w2b=w2b, w3b=w3b, W4=W4.astype(np.float64))
+
+
+def cv_gamma_mixed(params, time, paths, normals, payoffs, r):
+    """Gamma_p = payoff_p + sum_k e^{-r t_k} f(t_k, X_k) . dW_k at kernel
+    precision.  time (n, S), paths (n, S, d), normals (n, S, d)."""
+    n, S, d = normals.shape
+    out, _ = mlp_forward_mixed(params, np.reshape(time, -1), np.reshape(paths, (n * S, d)))
+    fo = out.reshape(n, S, d)
+    disc = np.exp(-np.asarray(time, np.float64).reshape(n, S) * r)
+    gam = np.asarray(payoffs, np.float64) + ((np.asarray(normals, np.float64) * fo).sum(-1) * disc).sum(-1)
+    return gam, fo
+
+
+def cv_grads_mixed(params, time, paths, normals, gamma, r):
+    """Gradients of Var(Gamma) (unbiased) at kernel precision, given Gamma."""
+    n, S, d = normals.shape
+    t = np.reshape(time, -1)
+    xin = np.reshape(paths, (n * S, d))
+    _, c = mlp_forward_mixed(params, t, xin)
+    g = np.asarray(gamma, np.float64)
+    dgam = 2.0 * (g - g.mean()) / (n - 1)
+    disc = np.exp(-np.asarray(time, np.float64).reshape(n, S) * r)
+    dO = ((dgam[:, None] * disc)[..., None] * np.asarray(normals, np.float64)).reshape(n * S, d)
+    dz3 = (dO @ c["W4"]) * (c["h3"] > 0)
+    gW4, gb4 = dO.T @ c["h3"], dO.sum(0)
+    dz3b = bf16_round(dz3).astype(np.float64)
+    gW3, gb3 = dz3b.T @ c["h2b"], dz3b.sum(0)
+    dz2b = bf16_round((dz3b @ c["w3b"]) * (c["h2b"] > 0)).astype(np.float64)
+    gW2, gb2 = dz2b.T @ c["h1b"], dz2b.sum(0)
+    dz1 = (dz2b @ c["w2b"]) * (c["h1b"] > 0)
+    inp = np.concatenate([np.asarray(t, np.float64)[:, None], np.asarray(xin, np.float64)], axis=1)
+    gW1, gb1 = dz1.T @ inp, dz1.sum(0)
+    return [gW1, gb1, gW2, gb2, gW3, gb3, gW4, gb4]

@@ -12,3 +12,5 @@ from .schemes import *
 from .solvers import *
 from .mc import *
 from .mlmc import *
+from .nets import *
+from .varred import *

@@ -80,6 +80,11 @@ _PROTOS = {
     "sdemc_batch_plan": (_I, [_P, _I, _P, ctypes.c_size_t]),
     "sdemc_batch_scratch_bytes": (ctypes.c_size_t, [_P]),
     "sdemc_price_batch": (_I, [_P, _P, _P, ctypes.c_size_t, _P, _P, _P, _I, _P]),
+    "sdemc_cv_nparams": (_I, [_I]),
+    "sdemc_cv_forward": (_I, [_I, _P, _P, _P, _P, _P, _P, ctypes.c_int64, _I, ctypes.c_float, _P, _P, _P]),
+    "sdemc_cv_backward": (_I, [_I, _P, _P, _P, _P, _P, ctypes.c_int64, _I, ctypes.c_float, _P, _P, _I, _P, _P]),
+    "sdemc_adam_step": (_I, [_P, _P, _P, _P, _I, _I, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                             ctypes.c_float, _P]),
     "sdemc_price_noalloc_scratch_bytes": (ctypes.c_size_t, []),
     "sdemc_price_noalloc": (_I, [_P, _P, _P, _P, _P]),
     "sdemc_replay": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),

@@ -150,7 +150,6 @@ def find_num_trials(problem, eps, models=None, init_trials=1e5, bs=1e5):
         stats = mc_simple(init_trials, problem.solver, problem.payoff, problem.discounter, bs,
                           payoff_time=payoff_time)
     else:
-        from .varred import mc_apply_cvs
         stats = mc_apply_cvs(models, problem.solver, init_trials, problem.payoff, problem.discounter, bs)
     ratio = (stats.sample_std * 1.96 / eps) ** 2
     return int(np.ceil(ratio * init_trials))
@@ -170,3 +169,144 @@ def run_mc(problem, eps, bs=1e5, init_trials=1e5):
 def run_mc_terminal_cv(problem, eps, bs=1e5, init_trials=1e5):
     trials = find_num_trials_terminal_cv(problem, eps, init_trials, bs)
     return mc_terminal_cv(trials, problem.solver, problem.payoff, problem.discounter, bs=bs)
+
+
+# ---------------------------------------------------- learned control variates
+def simulate_data(trials, solver, payoff, discounter, bs=1000, inference=False):
+    """Materialise paths, payoffs and normals into a DataLoader (diffusion
+    solvers; sde_mc/mc.py:378-388)."""
+    from torch.utils.data import DataLoader
+    from .nets import NormalPathData
+    if inference:
+        assert not trials % bs, 'Batch size should partition total trials evenly'
+    stats = mc_simple(trials, solver, payoff, discounter, return_normals=True)
+    dset = NormalPathData(stats.paths, stats.payoffs, stats.normals)
+    return DataLoader(dset, batch_size=int(bs), shuffle=not inference, drop_last=not inference)
+
+
+def simulate_adapted_data(trials, solver, payoff, discounter, bs=1000, inference=False):
+    """Materialise jump-adapted paths into AdaptedPathData (sde_mc/mc.py:391-398);
+    tensors stay on the GPU for the control-variate kernels."""
+    from torch.utils.data import DataLoader
+    from .nets import AdaptedPathData
+    if not is_jump_solver(solver):
+        raise ValueError("simulate_adapted_data needs a jump solver")
+    paths, aux, payoffs = materialise_with_payoffs(solver, int(trials), payoff, discounter, 'adapted')
+    normals, time_paths, left, total, jumps = aux
+    S = total
+    dset = AdaptedPathData(paths[:, :S + 1].contiguous(), payoffs, normals[:, :S].contiguous(),
+                           left[:, :S + 1], time_paths[:, :S + 1].contiguous(), jumps[:, :S + 1], S)
+    return DataLoader(dset, batch_size=int(bs), shuffle=not inference, drop_last=not inference)
+
+
+def sim_train_control_variates(models, opt, solver, trials, payoff, discounter, sim_bs, bs, epochs=10,
+                               print_losses=True, tol=0, early_stopping=None):
+    from .varred import train_adapted_control_variates, train_diffusion_control_variate
+    if solver.has_jumps:
+        dl = simulate_adapted_data(trials, solver, payoff, discounter, bs=bs)
+        return train_adapted_control_variates(models, opt, dl, solver, discounter, epochs, print_losses, tol,
+                                              early_stopping)
+    dl = simulate_data(trials, solver, payoff, discounter, bs=bs)
+    return train_diffusion_control_variate(models, opt, dl, solver, discounter, epochs, print_losses, tol,
+                                           early_stopping)[1]
+
+
+def mc_apply_cvs(models, solver, trials, payoff, discounter, sim_bs=1e5, bs=1000, tol=0):
+    """Plain estimate of Gamma = payoff + control variate over fresh paths
+    (sde_mc/mc.py:195-242)."""
+    from .helpers import mc_estimates
+    from .varred import apply_adapted_control_variates, apply_diffusion_control_variate
+    start = time.time()
+    trials = int(trials)
+    s = s2 = 0.0
+    left = trials
+    while left > 0:
+        n = int(min(sim_bs, left))
+        left -= n
+        if solver.has_jumps:
+            dl = simulate_adapted_data(n, solver, payoff, discounter, bs=bs, inference=True)
+            a, b = apply_adapted_control_variates(models, dl, solver, discounter, tol)
+        else:
+            dl = simulate_data(n, solver, payoff, discounter, bs=n, inference=True)
+            a, b = apply_diffusion_control_variate(models, dl, solver, discounter, tol)
+        s += float(a)
+        s2 += float(b)
+    mn, var = mc_estimates(s, s2, trials)
+    return MCStatistics(mn, math.sqrt(max(var, 0.0)) / math.sqrt(trials), time.time() - start, trials)
+
+
+def mc_adaptive_cv(models, opt, solver, trials, steps, payoff, discounter, sim_bs=(1e4, 1e4), bs=(1000, 1000),
+                   epochs=10, print_losses=True, pre_trained=False, tol=0, early_stopping=None):
+    """Train on a coarse grid, then estimate with the control variate on the
+    fine grid (sde_mc/mc.py:245-326)."""
+    from .varred import train_adapted_control_variates
+    train_trials, test_trials = trials
+    train_steps, test_steps = steps
+    train_bs, test_bs = bs
+    train_sim_bs, test_sim_bs = sim_bs
+    solver.num_steps = train_steps
+    if early_stopping is not None:
+        early_stopping.batch_size = bs[1]
+    t0 = time.time()
+    if not pre_trained:
+        dl = simulate_adapted_data(train_trials, solver, payoff, discounter, bs=train_bs)
+        train_adapted_control_variates(models, opt, dl, solver, discounter, epochs, print_losses, tol,
+                                       early_stopping=early_stopping)
+    train_time = time.time() - t0
+    solver.num_steps = test_steps
+    st = mc_apply_cvs(models, solver, test_trials, payoff, discounter, test_sim_bs, test_bs, tol)
+    st.time_elapsed += train_time
+    return st
+
+
+def mc_control_variates(models, opt, solver, trials, steps, payoff, discounter, sim_bs=(1e5, 1e5),
+                        bs=(1000, 1000), epochs=10, print_losses=True, tol=0, early_stopping=None):
+    """Diffusion-solver variant of mc_adaptive_cv (sde_mc/mc.py:126-192)."""
+    assert not solver.has_jumps
+    train_trials, test_trials = trials
+    train_steps, test_steps = steps
+    train_bs, test_bs = bs
+    train_sim_bs, test_sim_bs = sim_bs
+    solver.num_steps = train_steps
+    if early_stopping is not None:
+        early_stopping.batch_size = bs[1]
+    t0 = time.time()
+    sim_train_control_variates(models, opt, solver, train_trials, payoff, discounter, train_sim_bs, train_bs, epochs,
+                               print_losses, tol, early_stopping)
+    t1 = time.time()
+    solver.num_steps = test_steps
+    st = mc_apply_cvs(models, solver, test_trials, payoff, discounter, test_sim_bs, test_bs, tol)
+    st.time_elapsed += t1 - t0
+    return st
+
+
+def sample_batch_cost(solver, option, discounter, models, trials, bs, nn_bs):
+    out = mc_apply_cvs(models, solver, trials, option, discounter, bs, nn_bs)
+    return out.time_elapsed / (trials / nn_bs)
+
+
+def run_cv_mc(problem, models, opt, eps, train_size, step_factor=30, sim_bs=1e5, train_bs=1e3, nn_bs=1e3, epochs=10,
+              early_stopping=False, print_losses=True, init_trials=1e5):
+    """Train on a grid step_factor times coarser, size the run for a 95%
+    half-width eps from a pilot, then estimate with the control variate
+    (sde_mc/mc.py:443-467)."""
+    from .helpers import ceil_mult
+    from .varred import EarlyStopping
+    es = None
+    if early_stopping:
+        cost_batch = sample_batch_cost(problem.solver, problem.payoff, problem.discounter, models, sim_bs, sim_bs,
+                                       nn_bs)
+        es = EarlyStopping(eps, 1.96, cost_batch, 1)
+        es.batch_size = nn_bs
+    steps = problem.solver.num_steps
+    problem.solver.num_steps = int(np.ceil(steps / step_factor))
+    t0 = time.time()
+    sim_train_control_variates(models, opt, problem.solver, train_size, problem.payoff, problem.discounter, sim_bs,
+                               train_bs, epochs, print_losses, 0, es)
+    train_time = time.time() - t0
+    problem.solver.num_steps = steps
+    trials = ceil_mult(find_num_trials(problem, eps, models, init_trials, sim_bs), nn_bs)
+    st = mc_apply_cvs(models, problem.solver, trials, problem.payoff, problem.discounter, sim_bs, nn_bs)
+    test_time = st.time_elapsed
+    st.time_elapsed += train_time
+    return st, train_time, test_time

@@ -1,0 +1,273 @@
+"""Learned control variates with the reference's interface (sde_mc/varred.py).
+
+The Brownian integrand f of the adapted control variate
+    Gamma = payoff + sum_k e^{-r t_k} f(t_k, X_k) . dW_k
+is trained and evaluated on the GPU by the library's kernels (K5/K6): BF16
+tensor-core forward and backward passes with FP32 accumulation, a
+deterministic gradient reduction and a fused Adam step, all on paths the
+solver itself generated.  Training and inference run when the models are
+(``Mlp`` of the supported shape, ``ZeroFunction``) — the jump integrand g is
+not implemented and raises ``NotImplementedError``.
+"""
+import math
+import time
+
+import numpy as np
+import torch
+
+from . import _native as N
+from .helpers import partition, remove_steps
+from .nets import ZeroFunction
+
+
+class EarlyStopping:
+    """Stop training once the loss gain of an epoch no longer pays for its cost."""
+
+    def __init__(self, eps, quantile, cost_batch, alpha):
+        self.eps = eps
+        self.quantile = quantile
+        self.cost_batch = cost_batch
+        self.alpha = alpha
+        self.cost_epoch = None
+        self.batch_size = None
+
+    def threshold(self):
+        return self.alpha * (self.cost_epoch * self.eps ** 2 * self.batch_size) / (self.cost_batch * self.quantile ** 2)
+
+    def stop(self, delta_gamma):
+        return delta_gamma < self.threshold()
+
+
+def integrate_cv(normals, f_out, discounts, diffusion_struct, tol=0, time_interval=None):
+    """sum_k sum_i dW_{k,i} f_i discount_k (host torch helper, sde_mc/varred.py:202-214)."""
+    if tol != 0:
+        assert time_interval is not None
+        steps = normals.shape[1]
+        new_steps = remove_steps(tol, steps, time_interval)
+        normals, f_out, discounts = normals[:, :new_steps], f_out[:, :new_steps], discounts[:, :new_steps]
+    if diffusion_struct == 'diag':
+        return (normals * f_out * discounts).sum(-1).sum(-1)
+    return ((normals * f_out).sum(-1) * discounts).sum(-1).sum(-1)
+
+
+# --------------------------------------------------------------- GPU side --
+class CvData:
+    """Contiguous device tensors the kernels read: time (N, S+1), paths
+    (N, S+1, d), normals (N, S, d), discounted payoffs (N)."""
+
+    def __init__(self, time_full, paths_full, normals, payoffs, device):
+        self.time = time_full.to(device=device, dtype=torch.float32).contiguous()
+        self.paths = paths_full.to(device=device, dtype=torch.float32).contiguous()
+        self.normals = normals.to(device=device, dtype=torch.float32).contiguous()
+        self.payoffs = payoffs.to(device=device, dtype=torch.float32).contiguous()
+        self.n = int(self.payoffs.numel())
+        self.steps = int(self.normals.shape[1])
+        self.dim = int(self.normals.shape[2])
+        assert self.time.shape == (self.n, self.steps + 1)
+        assert self.paths.shape == (self.n, self.steps + 1, self.dim)
+
+    @classmethod
+    def from_dataset(cls, ds, solver, device):
+        if hasattr(ds, "full_time"):  # AdaptedPathData
+            return cls(ds.full_time.reshape(ds.full_time.shape[0], -1), ds.full_paths, ds.normals, ds.payoffs, device)
+        # NormalPathData (uniform grid): times from partition(T, steps, 'left')
+        n, steps = ds.normals.shape[0], ds.normals.shape[1]
+        tp = partition(solver.time_interval, steps, ends='left')
+        row = torch.cat([tp, torch.tensor([float(solver.time_interval)])]).to(torch.float32)
+        return cls(row.unsqueeze(0).expand(n, steps + 1), ds.full_paths, ds.normals, ds.payoffs, device)
+
+
+def kernel_models(models):
+    """(f, dim) when (f, g) are a supported Mlp and ZeroFunction, else raise."""
+    if isinstance(models, (list, tuple)):
+        f, g = models
+        if not isinstance(g, ZeroFunction):
+            raise NotImplementedError("the jump integrand g has no GPU kernel yet; pass ZeroFunction(d) as g")
+    else:
+        f = models
+    dim = f.kernel_dim() if hasattr(f, "kernel_dim") else None
+    if dim is None:
+        raise NotImplementedError("the GPU control-variate kernels implement Mlp(1+d, [64, 64, 64], d) with ReLU, "
+                                  "no batch norm, d in {1, 2}")
+    return f, dim
+
+
+def disc_rate(discounter):
+    r = getattr(discounter, "r", None)
+    if r is None:
+        raise NotImplementedError("control-variate kernels need a ConstantShortRate discounter")
+    return float(r)
+
+
+class GpuCv:
+    """Device state of one control-variate network: FP32 parameters, Adam
+    moments and the gradient workspace."""
+
+    def __init__(self, f, dim, device):
+        self.f, self.dim, self.device = f, dim, device
+        self.nparam = N.load().sdemc_cv_nparams(dim)
+        self.params = f.flat_params(device)
+        assert self.params.numel() == self.nparam
+        self.m = torch.zeros_like(self.params)
+        self.v = torch.zeros_like(self.params)
+        self.step_count = 0
+        self.grad = torch.zeros_like(self.params)
+        self.nparts = 2 * _sms()
+        self.partials = torch.empty((self.nparts, self.nparam), dtype=torch.float32, device=device)
+
+    def forward(self, data, rate, idx=None, gamma=None, fout=None):
+        n = data.n if idx is None else int(idx.numel())
+        if gamma is None:
+            gamma = torch.empty(n, dtype=torch.float32, device=self.device)
+        rc = N.load().sdemc_cv_forward(self.dim, N.ptr(self.params), N.ptr(data.time), N.ptr(data.paths),
+                                       N.ptr(data.normals), N.ptr(data.payoffs), N.ptr(idx), n, data.steps,
+                                       float(rate), N.ptr(gamma), N.ptr(fout), N.stream_handle(self.device))
+        N.check(rc, "sdemc_cv_forward")
+        return gamma
+
+    def backward(self, data, rate, gamma, idx=None):
+        n = data.n if idx is None else int(idx.numel())
+        rc = N.load().sdemc_cv_backward(self.dim, N.ptr(self.params), N.ptr(data.time), N.ptr(data.paths),
+                                        N.ptr(data.normals), N.ptr(idx), n, data.steps, float(rate), N.ptr(gamma),
+                                        N.ptr(self.partials), self.nparts, N.ptr(self.grad),
+                                        N.stream_handle(self.device))
+        N.check(rc, "sdemc_cv_backward")
+        return self.grad
+
+    def adam(self, lr=1e-3, betas=(0.9, 0.999), eps=1e-8):
+        self.step_count += 1
+        rc = N.load().sdemc_adam_step(N.ptr(self.params), N.ptr(self.grad), N.ptr(self.m), N.ptr(self.v),
+                                      self.nparam, self.step_count, float(lr), float(betas[0]), float(betas[1]),
+                                      float(eps), N.stream_handle(self.device))
+        N.check(rc, "sdemc_adam_step")
+
+    def write_back(self, opt=None):
+        """Copy the trained weights (and Adam state) into the torch objects."""
+        self.f.load_flat_params(self.params)
+        if opt is not None:
+            off = 0
+            for lin in self.f.linears():
+                for p in (lin.weight, lin.bias):
+                    n = p.numel()
+                    st = opt.state[p]
+                    st["step"] = torch.tensor(float(self.step_count))
+                    st["exp_avg"] = self.m[off:off + n].view_as(p).to(p.device).clone()
+                    st["exp_avg_sq"] = self.v[off:off + n].view_as(p).to(p.device).clone()
+                    off += n
+
+
+def _sms():
+    import ctypes
+    v = ctypes.c_int(0)
+    N.check(N.load().sdemc_device_sms(ctypes.byref(v)), "sdemc_device_sms")
+    return v.value
+
+
+def adam_hparams(opt):
+    if opt is None:
+        return 1e-3, (0.9, 0.999), 1e-8
+    if not isinstance(opt, torch.optim.Adam):
+        raise NotImplementedError("the GPU training step implements torch.optim.Adam")
+    grp = opt.param_groups[0]
+    if grp.get("weight_decay", 0) or grp.get("amsgrad", False) or grp.get("maximize", False):
+        raise NotImplementedError("Adam with weight decay / amsgrad / maximize is not implemented")
+    lr = grp["lr"]
+    return float(lr if not torch.is_tensor(lr) else lr.item()), tuple(grp["betas"]), float(grp["eps"])
+
+
+def train_gpu(cv, data, rate, epochs, batch_size, lr, betas, eps, print_losses=False, early_stopping=None,
+              generator=None):
+    """Minibatch training on device; returns the per-epoch mean losses."""
+    n = data.n
+    nb = n // batch_size
+    if nb < 1:
+        raise ValueError("batch size %d larger than the %d training paths" % (batch_size, n))
+    loss_arr = []
+    cost = 0.0
+    for epoch in range(epochs):
+        t0 = time.time()
+        perm = torch.randperm(n, device=cv.device, generator=generator)
+        losses = torch.zeros(nb, dtype=torch.float64, device=cv.device)
+        gamma = torch.empty(batch_size, dtype=torch.float32, device=cv.device)
+        for b in range(nb):
+            idx = perm[b * batch_size:(b + 1) * batch_size]
+            cv.forward(data, rate, idx, gamma)
+            losses[b] = gamma.double().var()
+            cv.backward(data, rate, gamma, idx)
+            cv.adam(lr, betas, eps)
+        loss_arr.append(float(losses.mean()))
+        if print_losses:
+            print('{}: Train loss: {:.5f}     95% confidence interval: {:.5f}'.format(
+                epoch, loss_arr[-1], np.sqrt(loss_arr[-1]) * 2 / np.sqrt(n)))
+        cost += time.time() - t0
+        if early_stopping is not None and epoch > 0:
+            early_stopping.cost_epoch = cost / (epoch + 1)
+            if early_stopping.stop(loss_arr[epoch - 1] - loss_arr[epoch]):
+                break
+    return loss_arr
+
+
+def _gpu_state(f, dim, device):
+    st = getattr(f, "_sdemc_gpu", None)
+    if st is None or st.device != device:
+        st = GpuCv(f, dim, device)
+        f._sdemc_gpu = st
+    else:
+        st.params = f.flat_params(device)
+    return st
+
+
+def train_adapted_control_variates(models, opt, dl, solver, discounter, epochs=10, print_losses=True, tol=0,
+                                   early_stopping=None):
+    """Train f on the dataset of ``dl`` (AdaptedPathData) with Adam; returns losses."""
+    if tol != 0:
+        raise NotImplementedError("tol != 0 (dropping the last steps) is not implemented on the GPU")
+    f, dim = kernel_models(models)
+    dev = N.require_cuda()
+    data = CvData.from_dataset(dl.dataset, solver, dev)
+    cv = _gpu_state(f, dim, dev)
+    lr, betas, eps = adam_hparams(opt)
+    losses = train_gpu(cv, data, disc_rate(discounter), epochs, int(dl.batch_size), lr, betas, eps, print_losses,
+                       early_stopping)
+    cv.write_back(opt)
+    return losses
+
+
+def apply_adapted_control_variates(models, dl, solver, discounter, tol=0):
+    """(sum Gamma, sum Gamma^2) over the dataset of ``dl``."""
+    if tol != 0:
+        raise NotImplementedError("tol != 0 is not implemented on the GPU")
+    f, dim = kernel_models(models)
+    dev = N.require_cuda()
+    data = CvData.from_dataset(dl.dataset, solver, dev)
+    cv = _gpu_state(f, dim, dev)
+    g = cv.forward(data, disc_rate(discounter)).double()
+    return g.sum(), (g * g).sum()
+
+
+def train_diffusion_control_variate(model, opt, dl, solver, discounter, epochs, print_losses=True, tol=0,
+                                    early_stopping=None):
+    """Uniform-grid variant (sde_mc/varred.py:23-72); returns (time, losses)."""
+    start = time.time()
+    if tol != 0:
+        raise NotImplementedError("tol != 0 is not implemented on the GPU")
+    f, dim = kernel_models(model)
+    dev = N.require_cuda()
+    data = CvData.from_dataset(dl.dataset, solver, dev)
+    cv = _gpu_state(f, dim, dev)
+    lr, betas, eps = adam_hparams(opt)
+    losses = train_gpu(cv, data, disc_rate(discounter), epochs, int(dl.batch_size), lr, betas, eps, print_losses,
+                       early_stopping)
+    cv.write_back(opt)
+    return time.time() - start, losses
+
+
+def apply_diffusion_control_variate(model, dl, solver, discounter, tol=0):
+    if tol != 0:
+        raise NotImplementedError("tol != 0 is not implemented on the GPU")
+    f, dim = kernel_models(model)
+    dev = N.require_cuda()
+    data = CvData.from_dataset(dl.dataset, solver, dev)
+    cv = _gpu_state(f, dim, dev)
+    g = cv.forward(data, disc_rate(discounter)).double()
+    return g.sum(), (g * g).sum()

@@ -1,0 +1,158 @@
+"""Control-variate network kernels (K5 forward, K6 backward, Adam) against the
+CPU oracle and the reference's own network, and what the trained network
+gains over the plain estimator.
+
+Tolerances: against the oracle's restatement of the kernels' precision policy
+(FP32 layers 1 and 4, BF16 64x64 layers with FP32 accumulation) the kernels
+agree to accumulation-order noise — outputs within 1e-3 of their largest
+magnitude, gradients within 3e-3 in relative norm.  Against the reference's
+FP32 network (fixture recorded from sde_mc) they agree to BF16 noise: 2%.
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+import sde_mc_gb300 as sm
+from sde_mc_gb300 import varred as V
+from tests.cases import indep2d, merton1d
+from tests.conftest import load_npz
+
+pytestmark = pytest.mark.gpu
+
+DEV = torch.device("cuda", 0)
+
+
+def _fixture():
+    fx = load_npz("cv_mlp")
+    n, S, d = fx["normals"].shape
+    t = torch.from_numpy(fx["time"][..., 0])
+    x = torch.from_numpy(fx["paths"])
+    # the kernels read (n, S+1) time and (n, S+1, d) paths: append a column
+    t_full = torch.cat([t, torch.ones(n, 1)], 1)
+    x_full = torch.cat([x, x[:, -1:]], 1)
+    data = V.CvData(t_full, x_full, torch.from_numpy(fx["normals"]), torch.from_numpy(fx["payoffs"]), DEV)
+    params = [fx["p0_%d" % i] for i in range(8)]
+    return fx, data, params
+
+
+def _net(d, params=None, seed=0):
+    torch.manual_seed(seed)
+    f = sm.Mlp(d + 1, [64, 64, 64], d, batch_norm=False, batch_norm_init=False)
+    if params is not None:
+        f.load_flat_params(torch.cat([torch.from_numpy(p).reshape(-1) for p in params]))
+    return f
+
+
+def test_forward_matches_oracle_and_reference(oracle_mod):
+    fx, data, params = _fixture()
+    n, S, d = fx["normals"].shape
+    cv = V.GpuCv(_net(d, params), d, DEV)
+    fout = torch.empty((n, S, d), dtype=torch.float32, device=DEV)
+    gamma = cv.forward(data, float(fx["r"]), fout=fout)
+    fo = fout.cpu().numpy().reshape(n * S, d)
+    mixed, _ = oracle_mod.mlp_forward_mixed(params, fx["time"].reshape(-1), fx["paths"].reshape(-1, d))
+    big = np.abs(mixed).max()
+    assert np.abs(fo - mixed).max() <= 1e-3 * big
+    assert np.abs(fo - fx["f_out"]).max() <= 2e-2 * np.abs(fx["f_out"]).max()
+    gm, fom = oracle_mod.cv_gamma_mixed(params, fx["time"][..., 0], fx["paths"], fx["normals"], fx["payoffs"],
+                                        float(fx["r"]))
+    scale = np.abs(fx["normals"] * fom).sum((1, 2))
+    g = gamma.cpu().numpy().astype(np.float64)
+    assert (np.abs(g - gm) <= 1e-3 * scale + 1e-6).all()
+    assert (np.abs(g - fx["gamma"]) <= 1e-2 * scale + 1e-6).all()
+
+
+def test_backward_matches_oracle_and_reference(oracle_mod):
+    fx, data, params = _fixture()
+    n, S, d = fx["normals"].shape
+    cv = V.GpuCv(_net(d, params), d, DEV)
+    gamma = torch.from_numpy(fx["gamma"]).to(DEV)
+    grad = cv.backward(data, float(fx["r"]), gamma).cpu().numpy()
+    mixed = oracle_mod.cv_grads_mixed(params, fx["time"][..., 0], fx["paths"], fx["normals"], fx["gamma"],
+                                      float(fx["r"]))
+    off = 0
+    for i in range(8):
+        m = mixed[i].reshape(-1)
+        g = grad[off:off + m.size]
+        off += m.size
+        assert np.linalg.norm(g - m) <= 3e-3 * np.linalg.norm(m) + 1e-9, ("oracle", i)
+        ref = fx["grad_%d" % i].reshape(-1)
+        assert np.linalg.norm(g - ref) <= 2e-2 * np.linalg.norm(ref) + 1e-9, ("reference", i)
+    assert off == grad.size
+    # deterministic: a second call gives the same bits
+    grad2 = cv.backward(data, float(fx["r"]), gamma).cpu().numpy()
+    np.testing.assert_array_equal(grad, grad2)
+
+
+def test_adam_step_matches_reference():
+    fx, data, params = _fixture()
+    d = fx["normals"].shape[2]
+    cv = V.GpuCv(_net(d, params), d, DEV)
+    cv.grad.copy_(torch.cat([torch.from_numpy(fx["grad_%d" % i]).reshape(-1) for i in range(8)]).to(DEV))
+    cv.adam(lr=1e-3)
+    new = cv.params.cpu().numpy()
+    ref = np.concatenate([fx["p1_%d" % i].reshape(-1) for i in range(8)])
+    np.testing.assert_allclose(new, ref, rtol=1e-6, atol=1e-7)
+
+
+def test_one_dimensional_network_and_index_gather(oracle_mod):
+    """d = 1 network on materialised Merton paths; a gather through an index
+    equals the forward on the gathered rows."""
+    solver, payoff, disc = merton1d(24, seed=7)
+    dl = sm.simulate_adapted_data(512, solver, payoff, disc, bs=512, inference=True)
+    data = V.CvData.from_dataset(dl.dataset, solver, DEV)
+    f = _net(1, seed=3)
+    cv = V.GpuCv(f, 1, DEV)
+    fout = torch.empty((data.n, data.steps, 1), dtype=torch.float32, device=DEV)
+    gamma = cv.forward(data, 0.02, fout=fout)
+    params = [p.detach().numpy() for lin in f.linears() for p in (lin.weight, lin.bias)]
+    S = data.steps
+    tt = data.time[:, :S].cpu().numpy()
+    xx = data.paths[:, :S].cpu().numpy()
+    gm, fom = oracle_mod.cv_gamma_mixed(params, tt, xx, data.normals.cpu().numpy(), data.payoffs.cpu().numpy(), 0.02)
+    assert np.abs(fout.cpu().numpy() - fom).max() <= 1e-3 * np.abs(fom).max()
+    scale = np.abs(data.normals.cpu().numpy() * fom).sum((1, 2))
+    assert (np.abs(gamma.cpu().numpy() - gm) <= 1e-3 * scale + 1e-6).all()
+    idx = torch.randperm(data.n, device=DEV)[:100]
+    g_idx = cv.forward(data, 0.02, idx=idx)
+    torch.testing.assert_close(g_idx, gamma[idx], rtol=0, atol=0)
+    # backward through the index equals backward on the gathered dataset
+    sub = V.CvData(data.time[idx], data.paths[idx], data.normals[idx], data.payoffs[idx], DEV)
+    g1 = cv.backward(data, 0.02, g_idx, idx=idx).clone()
+    g2 = cv.backward(sub, 0.02, g_idx).clone()
+    torch.testing.assert_close(g1, g2, rtol=0, atol=0)
+
+
+def test_training_reduces_variance_without_bias():
+    """Config-4 set-up at reduced size: the rainbow on two assets with
+    independent per-asset jumps.  Train on paths the solver generates, then
+    price fresh paths with and without the control variate: the variance
+    falls and the two means agree within 3 standard errors."""
+    solver, payoff, disc = indep2d(32, seed=11)
+    f = _net(2, seed=5)
+    opt = torch.optim.Adam(f.parameters(), lr=1e-3)
+    dl = sm.simulate_adapted_data(1 << 16, solver, payoff, disc, bs=1024)
+    losses = sm.train_adapted_control_variates([f, sm.ZeroFunction(2)], opt, dl, solver, disc, epochs=4,
+                                               print_losses=False)
+    assert losses[-1] < losses[0]
+    # the trained weights were written back to the torch module
+    assert torch.equal(f.flat_params(DEV), f._sdemc_gpu.params)
+    solver.seed = 99
+    st_cv = sm.mc_apply_cvs([f, sm.ZeroFunction(2)], solver, 1 << 16, payoff, disc, sim_bs=1 << 15, bs=1024)
+    st_plain = sm.mc_simple(1 << 16, solver, payoff, disc, bs=1 << 16, payoff_time='adapted')
+    vrf = (st_plain.sample_std / st_cv.sample_std) ** 2
+    assert vrf > 2.0, vrf
+    assert abs(st_cv.sample_mean - st_plain.sample_mean) < 3 * math.hypot(st_cv.sample_std, st_plain.sample_std)
+
+
+def test_unsupported_models_raise():
+    solver, payoff, disc = indep2d(8)
+    dl = sm.simulate_adapted_data(64, solver, payoff, disc, bs=64, inference=True)
+    g = sm.Mlp(3, [64, 64, 64], 2, batch_norm=False, batch_norm_init=False)
+    with pytest.raises(NotImplementedError):
+        sm.apply_adapted_control_variates([_net(2), g], dl, solver, disc)
+    with pytest.raises(NotImplementedError):
+        sm.apply_adapted_control_variates([sm.Mlp(3, [32, 32], 2, batch_norm=False, batch_norm_init=False),
+                                           sm.ZeroFunction(2)], dl, solver, disc)

@@ -128,6 +128,29 @@ def test_cv_mlp_grads_and_adam(oracle_mod):
         np.testing.assert_allclose(new[i], fx["p1_%d" % i], rtol=1e-5, atol=1e-6)
 
 
+def test_cv_mixed_precision_restatement_vs_reference(oracle_mod):
+    """The BF16 precision policy of the network kernels, restated on the CPU,
+    stays within BF16 noise of the reference's FP32 network: outputs within 2%
+    of their largest magnitude, every gradient within 2% in relative norm."""
+    fx = load_npz("cv_mlp")
+    p0 = [fx["p0_%d" % i] for i in range(8)]
+    n, S, d = fx["normals"].shape
+    out, _ = oracle_mod.mlp_forward_mixed(p0, fx["time"].reshape(-1), fx["paths"].reshape(-1, d))
+    assert np.abs(out - fx["f_out"]).max() <= 2e-2 * np.abs(fx["f_out"]).max()
+    gam, fo = oracle_mod.cv_gamma_mixed(p0, fx["time"][..., 0], fx["paths"], fx["normals"], fx["payoffs"],
+                                        float(fx["r"]))
+    scale = np.abs(fx["normals"] * fo).sum((1, 2))
+    assert (np.abs(gam - fx["gamma"]) <= 1e-2 * scale + 1e-6).all()
+    grads = oracle_mod.cv_grads_mixed(p0, fx["time"][..., 0], fx["paths"], fx["normals"], fx["gamma"],
+                                      float(fx["r"]))
+    for i in range(8):
+        ref = fx["grad_%d" % i]
+        assert np.linalg.norm(grads[i] - ref) <= 2e-2 * np.linalg.norm(ref), i
+    # bf16_round: ties to even, exact values unchanged
+    v = np.array([1.0, 1.0 + 2 ** -8, 1.0 + 3 * 2 ** -8, 1.0 + 2 ** -9, -2.5], np.float32)
+    np.testing.assert_array_equal(oracle_mod.bf16_round(v), [1.0, 1.0, 1.0 + 2 ** -6, 1.0, -2.5])
+
+
 def test_native_price_vs_merton_closed_form(oracle_mod, kat, ref_stats):
     """The oracle's own Philox draws through the reference loop price config 1
     within 3 standard errors of the Merton series and of the reference's run."""
