@@ -339,6 +339,90 @@ int sdemc_adam_step(float* d_params, const float* d_grad, float* d_m, float* d_v
                     int nparam, int step, float lr, float beta1, float beta2,
                     float eps, void* stream);
 
+/* ---- K9: pricing server (continuous batching) ---------------------------
+ * A request is one run_mc (sde_mc/mc.py:418-440): a pilot of inst.num_paths
+ * paths sizes the main run for a 95% half-width of rel_target * |price|
+ * (find_num_trials, :418-427), then the main run prices fresh paths.  The
+ * server owns one host thread, one CUDA stream (plus side streams) and its
+ * device memory.  Each request lives in a device-resident slot holding its
+ * descriptor, its RNG path counter and its FP64 running sums; every tick the
+ * thread packs a slice of every scheduled slot into per-dimension persistent
+ * kernels (same per-path code as K1), reduces each slot's chunk sums in a
+ * fixed order into its slot, and reads back only the slots that finished a
+ * phase.  Requests are admitted while slots and the device-memory budget
+ * allow; later arrivals join between ticks while others are running.
+ * A slot's slices depend only on its own request, so a result is the same
+ * bits whether the request ran alone or in any mix.
+ *
+ * Estimators: SDEMC_EST_PLAIN is the reference's plain estimator.
+ * SDEMC_EST_LINEAR_CV adds 2d control variates, per asset i
+ *   sum_k w_k X^i_k dW^i_k  and  sum_k w_k X^i_k (J^i_{k+1} - lambda_i E[J] dt_k),
+ * stochastic integrals against the Brownian increments and the compensated
+ * jump measure of the jump-adapted grid (mean exactly zero under the Euler
+ * scheme), with w_k a Black-Scholes delta of the payoff's underlying; their
+ * coefficients are fitted by regression on the pilot and the main run prices
+ * payoff - beta . r on fresh paths, so it stays unbiased.  Jump terms are on
+ * for lognormal marks (E[J] known exactly).  When the pilot shows no variance
+ * reduction the server falls back to the plain estimator; descriptors with
+ * non-diagonal noise or the payoff at the nominal step use the plain one. */
+enum { SDEMC_EST_PLAIN = 0, SDEMC_EST_LINEAR_CV = 1 };
+enum { SDEMC_SERVE_FIFO = 0, SDEMC_SERVE_SRPT = 1 };  /* tick fill order */
+
+typedef struct sdemc_server sdemc_server;
+
+typedef struct {
+  int32_t device;           /* CUDA device ordinal                              */
+  int32_t max_slots;        /* requests resident at once (1..65536)             */
+  int64_t mem_budget;       /* device bytes for slots and tick partials        */
+  int64_t tick_work;        /* path-step x dim units per tick (0: 2^33)         */
+  int64_t slice_work;       /* path-step x dim units per slot slice (0: 2^28)   */
+  int32_t block_threads;    /* class-kernel CTA size, multiple of 32 (0: 128)   */
+  int32_t side_streams;     /* class kernels spread over this many streams      */
+  int32_t policy;           /* SDEMC_SERVE_FIFO or SDEMC_SERVE_SRPT             */
+  int32_t reserved;
+} sdemc_server_cfg;
+
+typedef struct {
+  sdemc_inst inst;          /* num_paths = pilot paths; path_offset = first path */
+  double rel_target;        /* target 95% half-width / |price|                  */
+  int64_t max_paths;        /* cap on main-run paths (0: 2^36)                  */
+  uint64_t tag;             /* caller's id, returned with the result            */
+  int32_t estimator;        /* SDEMC_EST_*                                      */
+  int32_t reserved;
+} sdemc_request;
+
+typedef struct {
+  uint64_t tag;
+  int32_t status;           /* SDEMC_OK or an error code                        */
+  int32_t estimator;        /* estimator of the main run                        */
+  double mean, se;          /* main-run price and its standard error            */
+  double pilot_mean, pilot_se;
+  double vrf;               /* pilot variance / control-variate residual var.   */
+  int64_t pilot_paths, main_paths;
+  int64_t t_arrive_ns, t_admit_ns, t_done_ns;  /* CLOCK_MONOTONIC               */
+  float beta[2 * SDEMC_MAX_DIM];  /* control-variate coefficients (Brownian, jump) */
+} sdemc_result;
+
+typedef struct {
+  int64_t submitted, admitted, completed, pending, active;
+  int64_t ticks, mem_in_use, mem_peak;
+  int64_t path_steps;       /* executed path-steps (all slices)                 */
+  double busy_s;            /* sum of tick durations on the device              */
+} sdemc_server_stats;
+
+int sdemc_server_create(const sdemc_server_cfg* cfg, sdemc_server** out);
+/* Enqueue one request (thread-safe; arrival time = now).  Rejects invalid
+ * descriptors and requests that could never fit the budget.               */
+int sdemc_server_admit(sdemc_server* srv, const sdemc_request* req);
+/* Move up to max finished results into out; waits up to wait_ns for one.  */
+int sdemc_server_poll(sdemc_server* srv, sdemc_result* out, int max, int* n_out,
+                      int64_t wait_ns);
+int sdemc_server_stats_get(sdemc_server* srv, sdemc_server_stats* out);
+int sdemc_server_destroy(sdemc_server* srv);
+/* sizeof of sdemc_server_cfg, sdemc_request, sdemc_result and
+ * sdemc_server_stats (n >= 4), for bindings that mirror the structs.      */
+int sdemc_serve_sizes(size_t* out, int n);
+
 /* ---- RNG export (for the oracle and for users who want the raw draws) --
  * Philox4x32-10 blocks for counter (c0 = first_block + i, c1 = path lo,
  * c2 = path hi | tag << 16, c3 = stream_id), key = seed.                   */

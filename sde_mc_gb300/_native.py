@@ -95,6 +95,12 @@ _PROTOS = {
     "sdemc_mlmc_terminals": (_I, [_P, _I, _I, ctypes.c_float, ctypes.c_float, _P, _P, _P, _P]),
     "sdemc_mlmc_replay": (_I, [_P, _I, _I, ctypes.c_float, ctypes.c_float, _I, _I, _I, _I, _P, _P,
                                _P, _P, _P, _P, _P, _P]),
+    "sdemc_server_create": (_I, [_P, ctypes.POINTER(_P)]),
+    "sdemc_server_admit": (_I, [_P, _P]),
+    "sdemc_server_poll": (_I, [_P, _P, _I, ctypes.POINTER(_I), ctypes.c_int64]),
+    "sdemc_server_stats_get": (_I, [_P, _P]),
+    "sdemc_server_destroy": (_I, [_P]),
+    "sdemc_serve_sizes": (_I, [ctypes.POINTER(ctypes.c_size_t), _I]),
     "sdemc_philox": (_I, [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64,
                           ctypes.c_uint32, _I, _P, _P]),
     "sdemc_fp32_probe": (_I, [_I, _P, _I, ctypes.POINTER(ctypes.c_double), _P]),

@@ -166,6 +166,27 @@ def test_no_cpu_fallback():
         sm.mc_simple(1000, solver, payoff, disc, bs=1000)
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         solver.solve(8)
+    from sde_mc_gb300 import serve
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        serve.Server()
+
+
+def test_server_struct_layouts_match_header():
+    """The ctypes mirrors of the server's request/result structs have the C
+    sizes, and an invalid server configuration is refused before any device
+    work (no GPU needed)."""
+    import ctypes
+    from sde_mc_gb300 import serve
+    assert serve.struct_sizes() == (ctypes.sizeof(serve.ServerCfg), ctypes.sizeof(serve.Request),
+                                    ctypes.sizeof(serve.Result), ctypes.sizeof(serve.ServerStats))
+    assert serve.Request.inst.offset == 0 and ctypes.sizeof(serve.Request) == ctypes.sizeof(N.SdemcInst) + 32
+    lib = N.load()
+    h = ctypes.c_void_p()
+    bad = serve.ServerCfg(device=0, max_slots=0, mem_budget=1 << 30)
+    assert lib.sdemc_server_create(ctypes.byref(bad), ctypes.byref(h)) == N.EINVAL
+    assert h.value is None
+    bad = serve.ServerCfg(device=0, max_slots=4, mem_budget=1 << 30, block_threads=48)
+    assert lib.sdemc_server_create(ctypes.byref(bad), ctypes.byref(h)) == N.EINVAL
 
 
 def test_batch_plan_groups_and_orders():
