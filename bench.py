@@ -1,22 +1,30 @@
 #!/usr/bin/env python
-"""Benchmark: prices/s of the config-2 Levy rainbow at 1e-3 relative error.
+"""Benchmark: prices/s and p50/p99 latency of the served stream, served form
+(continuous batching + control variate) against the plain method.
 
-Workload (BASELINE config 2, one price = one plain Monte Carlo estimate whose
-95% half-width is 1e-3 of the price): 2D call on the max of two Merton assets
-with independent per-asset compound-Poisson jumps (rate 1.0 each, log-jumps
-N(-0.05, 0.15)), sigma = (0.2, 0.3), Brownian correlation 0.5, r = 0.02, T = 1,
-K = 1, 256 jump-adapted Euler steps, float32 state, FP64 cross-block sums.
-The path count N of one price comes from a 2^18-path pilot, as the reference's
-find_num_trials does (sde_mc/mc.py:418-427).  Inputs are synthetic by
-construction (the descriptor is the only input; paths are generated on the
-device), so L2 is flushed with a 256 MB write between timed steps.
+Headline workload (BASELINE config 5): pricing requests arrive as a Poisson
+process at 2000 req/s (numpy default_rng(1) exponential gaps); each request
+is a config-3 basket call (d ~ U{1..8}, steps log-U[32, 512], pilot paths =
+the instance's path count log-U[2^12, 2^18], K ~ U(0.8, 1.2), sigma_i ~
+U(0.1, 0.4), jump rate ~ U(0.5, 3), rho 0.3, log-jumps N(-0.1, 0.2)) with a
+target relative error drawn from {1e-2, 3e-3, 1e-3}; a request is one run_mc
+(pilot sizes the main run for a 95% half-width of target x |price|).  One
+step = the requests arriving in one 0.1 s window of that stream; the K timed
+windows are released back to back at their arrival times.
 
-One step = one price = K1 (fused paths + payoff + chunk sums) + K10 (FP64
-reduce) over N fresh paths.  `value` is device time (CUDA events, summed over
-the K timed steps); `e2e` calls the public API mc_simple(...) with host objects
-every step (descriptor lowering, launch parameters host->device, 48-byte
-result device->host, MCStatistics).  `--impl reference` times the CPU
-restatement of the reference's algorithm on the host cores.
+* `value`: requests / device busy time of the server's ticks (the kernels,
+  uploads and readbacks the server enqueued; inputs are descriptors).
+* `e2e`: requests / wall time from the first arrival to the last result,
+  through the public API (descriptors submitted from the host, results read
+  back to the host); latencies are arrival -> result.
+* `plain`: the same stream served by the plain method one request at a time
+  (pilot K1 launch + readback, main K1 launch + readback).
+* `c2_plain`: config 2 (2D rainbow at 1e-3 relative error) with K1 — the
+  per-path kernel every form shares — and its FP32 roofline.
+* `c2_mlmc`, `batched_mix` (config 3), `cv_learned` (config 4): the other
+  forms, measured once.
+`--impl reference` prices the same stream's requests with the CPU
+restatement of the reference's algorithm (oracle port) on all host cores.
 """
 import argparse
 import json
@@ -33,34 +41,36 @@ sys.path.insert(0, ROOT)
 
 METRIC = "prices/s and p50/p99 latency at 1e-3 rel. error: CV+batched+served vs plain"
 UNIT = "prices/s"
-WORKLOAD = ("config-2 2D rainbow (call on max), Merton assets with independent per-asset jumps "
-            "(rate 1.0, logN(-0.05,0.15)), sigma (0.2,0.3), rho 0.5, r 0.02, T 1, K 1, 256 jump-adapted steps; "
-            "one price = plain MC at 1e-3 relative 95% half-width")
+RATE = 2000.0
+WINDOW_S = 0.1
+WORKLOAD = ("config-5 served stream: Poisson arrivals at 2000 req/s (default_rng(1) exponential gaps), each a "
+            "config-3 basket call (d~U{1..8}, steps log-U[32,512], pilot paths log-U[2^12,2^18], K~U(0.8,1.2), "
+            "sigma_i~U(0.1,0.4), jump rate~U(0.5,3), rho 0.3, logN(-0.1,0.2) jumps, r 0.02, T 1) with target "
+            "relative error from {1e-2,3e-3,1e-3}; one step = the requests of one 0.1 s window of the stream")
+C2_WORKLOAD = ("config-2 2D rainbow (call on max), Merton assets with independent per-asset jumps "
+               "(rate 1.0, logN(-0.05,0.15)), sigma (0.2,0.3), rho 0.5, r 0.02, T 1, K 1, 256 jump-adapted steps; "
+               "one price = plain MC at 1e-3 relative 95% half-width")
+MIX_WORKLOAD = ("config-3 mix: 512 correlated Merton basket calls, d~U{1..8}, steps log-U[32,512], "
+                "paths log-U[2^12,2^18], K~U(0.8,1.2), sigma_i~U(0.1,0.4), rate~U(0.5,3), rho 0.3, "
+                "logN(-0.1,0.2) jumps; numpy default_rng(0)")
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--rel", type=float, default=1e-3)
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--plain-windows", type=int, default=10,
+                    help="windows of the stream the plain one-request-per-launch server replays")
+    ap.add_argument("--sections", default="c2,mlmc,mix,cv",
+                    help="extra sections measured once: c2, mlmc, mix, cv (comma list, or 'none')")
     ap.add_argument("--profile-paths", type=int, default=0,
-                    help="profiling driver: make three price launches of the workload at this many paths "
-                         "and exit (the case ncu captures)")
+                    help="profiling driver: three config-2 price launches at this many paths, then exit")
+    ap.add_argument("--profile-serve", type=float, default=0.0,
+                    help="profiling driver: serve this many seconds of the stream, then exit")
     return ap.parse_args()
-
-
-def profile_launches(n):
-    import torch
-    from sde_mc_gb300 import kernels as K
-    from sde_mc_gb300.lowering import lower
-    solver, payoff, disc = make_problem()
-    for i in range(3):
-        r = K.price(lower(solver, payoff, disc, num_paths=n, path_offset=i * n, seed=1))
-    torch.cuda.synchronize()
-    print(json.dumps({"profile_paths": n, "result": r.cpu().tolist()}))
 
 
 def dist_env():
@@ -137,76 +147,212 @@ def algorithmic_flops_per_path_step(d):
     return 5 + 10 * d + (d * (d + 1) if d > 1 else 0)
 
 
-def load_peaks():
-    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    if os.path.exists(p):
-        with open(p) as fh:
-            return json.load(fh)
-    return {}
-
-
-def load_profile_traffic():
-    p = os.path.join(ROOT, "profiles", "price_kernel_traffic.json")
+def load_json_file(name):
+    p = os.path.join(ROOT, name)
     if os.path.exists(p):
         with open(p) as fh:
             return json.load(fh)
     return None
 
 
-def cpu_sample(inst_factory, n_target, budget_s):
-    """Time the oracle port (C, all host threads) on a bounded sample of paths."""
+def fp32_peak_tflops(dev):
+    """Measured FFMA throughput of this GPU (best of 6 probe launches)."""
+    import ctypes
+    import torch
+    from sde_mc_gb300 import _native as N
+    lib = N.load()
+    sink = torch.zeros(16, dtype=torch.float32, device=dev)
+    fl = ctypes.c_double(0.0)
+    best = 0.0
+    s = N.stream_handle(dev)
+    for _ in range(6):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        N.check(lib.sdemc_fp32_probe(4096, N.ptr(sink), 16, ctypes.byref(fl), s), "fp32 probe")
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, fl.value / (e0.elapsed_time(e1) * 1e-3))
+    return best / 1e12
+
+
+def stream_windows(first, count):
+    """Requests of windows [first, first + count) of the stream, times relative
+    to the start of window `first`."""
+    from sde_mc_gb300 import stream as S
+    return S.make_stream(RATE, (first + count) * WINDOW_S, seed=1, t_begin=first * WINDOW_S)
+
+
+def oracle_serve(stream, budget_s, threads=None):
+    """The plain method on the host cores through the oracle port (the CPU
+    restatement of the reference's algorithm, all threads), request by request
+    in arrival order until budget_s is spent.  A main run longer than its
+    share of the budget is timed on a prefix of its paths and extrapolated
+    linearly (CPU time is proportional to paths).  Returns (seconds per
+    request, requests timed, threads, paths timed)."""
     from oracle import oracle
-    threads = os.cpu_count() or 1
-    n = 4096
-    while True:
-        inst = inst_factory(n)
-        t0 = time.perf_counter()
-        oracle.price(inst, nthreads=threads)
-        dt = time.perf_counter() - t0
-        if dt > budget_s / 4 or n >= n_target:
+    threads = threads or os.cpu_count() or 1
+    spent, times, paths = 0.0, [], 0
+    for r in stream:
+        if spent >= budget_s and times:
             break
-        n = min(n_target, int(n * min(8.0, max(2.0, budget_s / 4 / max(dt, 1e-3)))))
-    paths_per_s = n / dt
-    return paths_per_s, n, dt, threads
+        n0 = int(r.inst.num_paths)
+        t = time.perf_counter()
+        out, _, _ = oracle.price(r.phase(n0, 0), nthreads=threads)
+        t_pilot = time.perf_counter() - t
+        mean0, var0 = float(out[3]), float(out[4])
+        eps = r.target * abs(mean0)
+        n = max(64, math.ceil(1.96 ** 2 * var0 / eps ** 2)) if var0 > 0 and eps > 0 else 0
+        per_path = t_pilot / max(n0, 1)
+        share = max(budget_s / 6.0, 0.5)
+        m = min(n, n if n * per_path <= share else max(4096, int(share / max(per_path, 1e-12))))
+        t_main = 0.0
+        if m > 0:
+            t = time.perf_counter()
+            oracle.price(r.phase(m, n0), nthreads=threads)
+            dt = time.perf_counter() - t
+            t_main = dt * (n / m)
+            spent += dt
+        spent += t_pilot
+        paths += n0 + m
+        times.append(t_pilot + t_main)
+    return statistics.mean(times), len(times), threads, paths
 
 
 def run_reference(args):
+    """`--impl reference`: the stream's requests priced by the plain method on
+    the host cores (oracle port); one step = one bounded sample of requests."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    import torch
-    from sde_mc_gb300.lowering import lower
-    solver, payoff, disc = make_problem()
-    # N for one price: from the pilot statistics the GPU arm uses (same model)
-    n_target = int(os.environ.get("SDEMC_BENCH_N", "6200000"))
-
-    def factory(n):
-        return lower(solver, payoff, disc, num_paths=n, path_offset=0, seed=1)
-    per_step = max(args.cpu_seconds / max(args.steps + args.warmup, 1), 0.5)
-    times = []
-    n_used = 0
-    threads = os.cpu_count() or 1
+    from sde_mc_gb300 import stream as S
+    reqs = S.make_stream(RATE, 0.05, seed=1)
+    per_step = max(args.cpu_seconds / max(args.steps + args.warmup, 1), 1.0)
+    secs, n_req, threads = [], 0, os.cpu_count() or 1
+    pos = 0
     for i in range(args.warmup + args.steps):
-        pps, n, dt, threads = cpu_sample(factory, n_target, per_step)
+        chunk = reqs[pos:] + reqs[:pos]
+        spr, n, threads, _ = oracle_serve(chunk, per_step)
+        pos = (pos + n) % len(reqs)
         if i >= args.warmup:
-            times.append(n_target / pps)
-            n_used = n
-    sec_per_price = statistics.mean(times)
+            secs.append(spr)
+            n_req += n
+    sec_per_price = statistics.mean(secs)
     value = 1.0 / sec_per_price
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec_per_price * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": {"workload": WORKLOAD, "paths_per_price": n_target},
+            "data": "synthetic", "config": {"workload": WORKLOAD, "form": "plain run_mc per request"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": "%d paths per step timed on %d threads, extrapolated to %d paths per price"
-                                       % (n_used, threads, n_target)},
+                             "sample": "%d stream requests (pilot + main, plain estimator) on %d threads; main "
+                                       "runs over their share of %.1f s per step timed on a prefix of paths and "
+                                       "extrapolated" % (n_req, threads, per_step)},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
-MIX_WORKLOAD = ("config-3 mix: 512 correlated Merton basket calls, d~U{1..8}, steps log-U[32,512], "
-                "paths log-U[2^12,2^18], K~U(0.8,1.2), sigma_i~U(0.1,0.4), rate~U(0.5,3), rho 0.3, "
-                "logN(-0.1,0.2) jumps; numpy default_rng(0)")
+# ------------------------------------------------------------ sections ----
+def bench_c2_plain(dev, steps, warmup, fp32_peak):
+    """Config 2 at 1e-3 relative error with K1 (+K10), device-timed, L2
+    flushed between steps; the FP32 roofline of price_kernel<2>."""
+    import ctypes
+    import torch
+    import sde_mc_gb300 as sm
+    from sde_mc_gb300 import _native as N
+    from sde_mc_gb300 import kernels as K
+    from sde_mc_gb300.lowering import lower
+    solver, payoff, disc = make_problem()
+    lib = N.load()
+    pilot = K.price(lower(solver, payoff, disc, num_paths=1 << 18, path_offset=0, seed=7)).cpu().tolist()
+    price, var = pilot[3], pilot[4]
+    n_target = int(math.ceil((1.96 * math.sqrt(var) / (1e-3 * price)) ** 2))
+    n_target = (n_target + 127) // 128 * 128
+    m = K.materialise(lower(solver, payoff, disc, num_paths=1 << 14, path_offset=1 << 40, seed=7),
+                      solver.num_steps + solver.max_jumps, want=("steps",))
+    steps_per_path = float(m["steps"].double().mean())
+    flops = n_target * steps_per_path * algorithmic_flops_per_path_step(2)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    need = lib.sdemc_price_scratch_bytes(ctypes.byref(lower(solver, payoff, disc, num_paths=n_target)))
+    scratch = N.SCRATCH.get(need, dev)
+    out = torch.empty(6, dtype=torch.float64, device=dev)
+    nch = (n_target + N.CHUNK_PATHS - 1) // N.CHUNK_PATHS
+    s = N.stream_handle(dev)
+
+    def one(i, ev=None):
+        inst = lower(solver, payoff, disc, num_paths=n_target, path_offset=(i + 1) * n_target, seed=1)
+        if ev:
+            ev[0].record()
+        N.check(lib.sdemc_price_chunks(ctypes.byref(inst), None, N.ptr(scratch), scratch.numel(), None, s), "chunks")
+        if ev:
+            ev[1].record()
+        N.check(lib.sdemc_reduce_chunks(N.ptr(scratch), nch, 3, N.ptr(out), s), "reduce")
+        if ev:
+            ev[2].record()
+
+    for i in range(warmup):
+        one(i)
+    torch.cuda.synchronize()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
+    res = []
+    for i in range(steps):
+        flush.fill_(i & 0xFF)
+        one(warmup + i, evs[i])
+        res.append(out.clone())
+    torch.cuda.synchronize()
+    k_ms = [e[0].elapsed_time(e[1]) for e in evs]
+    r_ms = [e[1].elapsed_time(e[2]) for e in evs]
+    rows = [r.cpu().tolist() for r in res]
+    for r in rows:
+        N.status_error(r[5], "bench c2")
+    e2e = []
+    for i in range(warmup + min(steps, 10)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sm.mc_simple(n_target, solver, payoff, disc, bs=n_target, payoff_time='adapted')
+        if i >= warmup:
+            e2e.append(time.perf_counter() - t0)
+    kernel_s = statistics.mean(k_ms) * 1e-3
+    achieved = flops / kernel_s / 1e12
+    traffic = load_json_file(os.path.join("profiles", "price_kernel_traffic.json"))
+    return {"workload": C2_WORKLOAD, "paths_per_price": n_target, "steps_per_path": steps_per_path,
+            "prices_per_s": steps / (sum(k_ms) + sum(r_ms)) * 1e3, "ms_per_price": statistics.mean(
+                [a + b for a, b in zip(k_ms, r_ms)]),
+            "e2e_prices_per_s": len(e2e) / sum(e2e), "price": statistics.mean(r[3] for r in rows),
+            "rel_halfwidth": statistics.mean(1.96 * math.sqrt(r[4] / r[2]) / r[3] for r in rows),
+            "path_steps_per_s": n_target * steps_per_path / kernel_s,
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                         "frac": achieved / fp32_peak,
+                         "traffic": (traffic["bytes_per_path"] * n_target) if traffic else None,
+                         "kernel": "price_kernel<2,diag>", "kernel_ms": kernel_s * 1e3,
+                         "flops_per_path_step": algorithmic_flops_per_path_step(2),
+                         "peak_source": "measured FFMA probe on this GPU (sdemc_fp32_probe)"},
+            "l2": "flushed (256 MB write) between timed steps", "gpu_launches": 2 * steps}
+
+
+def bench_c2_mlmc(dev):
+    """Config 2 with MLMC (levels 0..6, 2^(l+2) steps) at eps = 1e-3 x price:
+    Giles' allocation from a 2^14-path pilot per level, then one run."""
+    import torch
+    import sde_mc_gb300 as sm
+    solver, payoff, disc = make_problem()
+    levels = [2 ** (l + 2) for l in range(7)]
+    ref = sm.mc_simple(1 << 20, solver, payoff, disc, bs=1 << 20, payoff_time='adapted')
+    eps = 1e-3 * ref.sample_mean
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    trials = sm.get_optimal_trials(1 << 14, levels, eps, solver, payoff, disc)
+    t_pilot = time.perf_counter() - t0
+    times = []
+    for i in range(4):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st = sm.mc_multilevel(trials, levels, solver, payoff, disc)
+        times.append(time.perf_counter() - t0)
+    run_s = statistics.mean(times[1:])
+    fine_steps = sum(n * (lv + 1.0) for n, lv in zip(trials, levels))
+    return {"levels": levels, "trials": trials, "eps": eps, "price": st.sample_mean,
+            "halfwidth": 1.96 * st.sample_std, "prices_per_s": 1.0 / run_s,
+            "prices_per_s_with_pilot": 1.0 / (run_s + t_pilot), "path_steps_fine_equiv": fine_steps,
+            "note": "MLMC estimates E[P_L] at L = 256 steps (level 6); plain c2 prices the same target"}
 
 
 def bench_batched_mix(steps, warmup):
@@ -218,12 +364,11 @@ def bench_batched_mix(steps, warmup):
     from sde_mc_gb300 import workloads
     mix = workloads.basket_mix(512)
     n = len(mix)
-    offs = [0] * n
-    insts = B.lower_mix(mix, offs)
+    insts = B.lower_mix(mix, [0] * n)
     plan = B.BatchPlan(insts)
     tune = B.autotune(plan, repeats=2)
     steps = max(1, min(steps, 10))
-    plan.set_path_offsets([(1 << 40) + m.paths * 0 for m in mix])
+    plan.set_path_offsets([1 << 40 for _ in mix])
     plan.run()
     torch.cuda.synchronize()
     graph = torch.cuda.CUDAGraph()
@@ -242,7 +387,6 @@ def bench_batched_mix(steps, warmup):
             ms.append(e0.elapsed_time(e1))
     rows = plan.out[:n].cpu().numpy()
     batched_ms = sum(ms) / len(ms)
-    # plain: one request per launch, descriptors lowered ahead of time
     plain_insts = B.lower_mix(mix, [(1 << 41)] * n)
     outs = [torch.empty(6, dtype=torch.float64, device="cuda") for _ in range(n)]
     pm = []
@@ -268,153 +412,185 @@ def bench_batched_mix(steps, warmup):
             "status_ok": bool((rows[:, 5] == 0).all())}
 
 
+def bench_cv_learned(dev, epochs=10):
+    """Config 4: the learned control variate on the config-2 model — train
+    Mlp(3, [64, 64, 64], 2) with Adam (lr 1e-3, batch 4096) on 2^18 paths the
+    solver generates (K4 + K5/K6), evaluate on 2^22 fresh paths (K4 + K5);
+    VRF against the plain estimator on the same fresh paths and the bias."""
+    import torch
+    import sde_mc_gb300 as sm
+    solver, payoff, disc = make_problem()
+    torch.manual_seed(0)
+    f = sm.Mlp(3, [64, 64, 64], 2, batch_norm=False, batch_norm_init=False)
+    opt = torch.optim.Adam(f.parameters(), lr=1e-3)
+    models = [f, sm.ZeroFunction(2)]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    dl = sm.simulate_adapted_data(1 << 18, solver, payoff, disc, bs=4096)
+    torch.cuda.synchronize()
+    t_sim = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    losses = sm.train_adapted_control_variates(models, opt, dl, solver, disc, epochs=epochs, print_losses=False)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    del dl
+    n_eval = 1 << 22
+    start = solver.path_cursor
+    t0 = time.perf_counter()
+    st_cv = sm.mc_apply_cvs(models, solver, n_eval, payoff, disc, sim_bs=1 << 18, bs=4096)
+    torch.cuda.synchronize()
+    t_eval = time.perf_counter() - t0
+    plain = sm.price_stats(solver, payoff, disc, n_eval, payoff_time='adapted', path_offset=start)
+    mean_p, se_p, _ = sm.finish_stats(plain)
+    vrf = (se_p / st_cv.sample_std) ** 2
+    bias = st_cv.sample_mean - mean_p
+    return {"workload": "config-4 learned CV on the config-2 model, Mlp(3,[64,64,64],2) ReLU no BN, Adam lr 1e-3 "
+                        "batch 4096, %d epochs on 2^18 solver paths, evaluated on 2^22 fresh paths" % epochs,
+            "vrf": vrf, "mean_cv": st_cv.sample_mean, "se_cv": st_cv.sample_std, "mean_plain": mean_p,
+            "se_plain": se_p, "bias": bias, "bias_in_se": bias / math.hypot(st_cv.sample_std, se_p),
+            "loss_first_last": [losses[0], losses[-1]], "simulate_s": t_sim, "train_s": t_train, "eval_s": t_eval,
+            "note": "the plain estimate uses the same 2^22 fresh paths as the control-variate estimate"}
+
+
+def bench_served(dev, steps, warmup, plain_windows):
+    """The headline: K windows of the served stream through the server, and
+    the plain one-request-per-launch server on the first windows."""
+    import torch
+    from sde_mc_gb300 import serve
+    from sde_mc_gb300 import stream as S
+    srv = serve.Server(max_slots=4096, mem_budget=40 << 30, side_streams=4, policy="srpt", device=dev)
+    warm = stream_windows(0, warmup)
+    S.run_served(warm, srv)
+    timed = stream_windows(warmup, steps)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    flush.fill_(1)
+    torch.cuda.synchronize()
+    st0 = srv.stats()
+    res, summ = S.run_served(timed, srv)
+    st1 = srv.stats()
+    srv.close()
+    busy = st1["busy_s"] - st0["busy_s"]
+    delta = {k: st1[k] - st0[k] for k in ("ticks", "launches", "h2d_bytes", "d2h_bytes", "path_steps")}
+    flops = 0.0
+    for r in timed:
+        x = res[r.idx]
+        flops += (x.pilot_paths + x.main_paths) * r.path_steps * algorithmic_flops_per_path_step(r.dim)
+    plain_reqs = [r for r in timed if r.t < min(steps, plain_windows) * WINDOW_S]
+    S.run_plain(warm[:50])
+    _, psumm = S.run_plain(plain_reqs)
+    # price agreement between the two servers (each within its own error)
+    return {"summary": summ, "busy_s": busy, "delta": delta, "flops": flops, "plain": psumm,
+            "plain_windows": min(steps, plain_windows), "results": res, "timed": timed}
+
+
+def profile_serve(seconds):
+    import torch
+    from sde_mc_gb300 import serve
+    from sde_mc_gb300 import stream as S
+    reqs = S.make_stream(RATE, seconds, seed=1)
+    with serve.Server(max_slots=4096, mem_budget=40 << 30, side_streams=4) as srv:
+        _, summ = S.run_served(reqs, srv)
+        summ["stats"] = srv.stats()
+    torch.cuda.synchronize()
+    print(json.dumps(summ))
+
+
+def profile_launches(n):
+    import torch
+    from sde_mc_gb300 import kernels as K
+    from sde_mc_gb300.lowering import lower
+    solver, payoff, disc = make_problem()
+    for i in range(3):
+        r = K.price(lower(solver, payoff, disc, num_paths=n, path_offset=i * n, seed=1))
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_paths": n, "result": r.cpu().tolist()}))
+
+
+def _section(fn, *a):
+    try:
+        return fn(*a)
+    except Exception as e:  # an auxiliary section must not hide the headline
+        return {"error": "%s: %s" % (type(e).__name__, e)}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
     if args.profile_paths:
         return profile_launches(args.profile_paths)
+    if args.profile_serve:
+        return profile_serve(args.profile_serve)
     import torch
     import torch.distributed as dist
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    import ctypes
-    import sde_mc_gb300 as sm
-    from sde_mc_gb300 import _native as N
-    from sde_mc_gb300 import kernels as K
-    from sde_mc_gb300.lowering import lower
-
-    solver, payoff, disc = make_problem()
     dev = torch.device("cuda", local)
-    lib = N.load()
-
-    # pilot -> paths per price for the target relative error
-    pilot = K.price(lower(solver, payoff, disc, num_paths=1 << 18, path_offset=0, seed=7)).cpu().tolist()
-    price, var = pilot[3], pilot[4]
-    n_target = int(math.ceil((1.96 * math.sqrt(var) / (args.rel * price)) ** 2))
-    n_target = (n_target + 127) // 128 * 128
-
-    # mean executed steps per path (jump-adapted grid: 256 + jumps + end steps)
-    m = K.materialise(lower(solver, payoff, disc, num_paths=1 << 14, path_offset=1 << 40, seed=7),
-                      solver.num_steps + solver.max_jumps, want=("steps",))
-    steps_per_path = float(m["steps"].double().mean())
-    path_steps = n_target * steps_per_path
-    flops = path_steps * algorithmic_flops_per_path_step(2)
-
-    # measured FP32 peak (FFMA chains at full occupancy), best of 5
-    sink = torch.zeros(16, dtype=torch.float32, device=dev)
-    fl = ctypes.c_double(0.0)
-    best = 0.0
-    s = N.stream_handle(dev)
-    for _ in range(6):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        N.check(lib.sdemc_fp32_probe(4096, N.ptr(sink), 16, ctypes.byref(fl), s), "fp32 probe")
-        e1.record()
-        torch.cuda.synchronize()
-        best = max(best, fl.value / (e0.elapsed_time(e1) * 1e-3))
-    fp32_peak_tflops = best / 1e12
-
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    need = lib.sdemc_price_scratch_bytes(ctypes.byref(lower(solver, payoff, disc, num_paths=n_target)))
-    scratch = N.SCRATCH.get(need, dev)
-    out = torch.empty(6, dtype=torch.float64, device=dev)
-    nch = (n_target + N.CHUNK_PATHS - 1) // N.CHUNK_PATHS
-    base = rank * (1 << 44)
-
-    def one_step(i, ev=None):
-        inst = lower(solver, payoff, disc, num_paths=n_target, path_offset=base + (i + 1) * n_target, seed=1)
-        if ev:
-            ev[0].record()
-        N.check(lib.sdemc_price_chunks(ctypes.byref(inst), None, N.ptr(scratch), scratch.numel(), None, s), "chunks")
-        if ev:
-            ev[1].record()
-        N.check(lib.sdemc_reduce_chunks(N.ptr(scratch), nch, 3, N.ptr(out), s), "reduce")
-        if ev:
-            ev[2].record()
-
-    for i in range(args.warmup):
-        one_step(i)
-    torch.cuda.synchronize()
-    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
-    results = []
+    fp32_peak = fp32_peak_tflops(dev)
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        w0 = time.perf_counter()
-        for i in range(args.steps):
-            flush.fill_(i & 0xFF)
-            one_step(args.warmup + i, evs[i])
-            results.append(out.clone())
-        torch.cuda.synchronize()
-        wall = time.perf_counter() - w0
+        b = bench_served(dev, args.steps, args.warmup, args.plain_windows)
     if world > 1:
         dist.barrier()
-    k_ms = [e[0].elapsed_time(e[1]) for e in evs]
-    r_ms = [e[1].elapsed_time(e[2]) for e in evs]
-    step_ms = [a + b for a, b in zip(k_ms, r_ms)]
-    total_s = sum(step_ms) * 1e-3
+    summ, busy = b["summary"], b["busy_s"]
+    n_req = summ["requests"]
+    wall = summ["seconds"]
     if world > 1:
-        t = torch.tensor([total_s], device=dev)
+        t = torch.tensor([busy, wall], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
-    value = world * args.steps / total_s
-    res = [r.cpu().tolist() for r in results]
-    for r in res:
-        N.status_error(r[5], "bench")
-    rel_err = statistics.mean(1.96 * math.sqrt(r[4] / r[2]) / r[3] for r in res)
-
-    # end to end through the public API (host objects in, Python floats out)
-    e2e_t = []
-    for i in range(args.warmup + args.steps):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        st = sm.mc_simple(n_target, solver, payoff, disc, bs=n_target, payoff_time='adapted')
-        if i >= args.warmup:
-            e2e_t.append(time.perf_counter() - t0)
-    e2e_value = world * len(e2e_t) / sum(e2e_t) if world == 1 else None
-    if world > 1:
-        t = torch.tensor([sum(e2e_t)], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_value = world * len(e2e_t) / float(t.item())
-
-    kernel_s = statistics.mean(k_ms) * 1e-3
-    achieved = flops / kernel_s / 1e12
-    traffic = load_profile_traffic()
+        busy, wall = float(t[0]), float(t[1])
+    value = world * n_req / busy
+    e2e = world * n_req / wall
+    achieved = b["flops"] / busy / 1e12
+    plain = b["plain"]
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": busy * 1e3 / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "paths_per_price": n_target, "form": "plain",
-                   "steps_per_path": steps_per_path, "l2": "flushed (256 MB write) between timed steps",
+        "config": {"workload": WORKLOAD, "form": "served: continuous-batching server (SRPT ticks, 4 side streams, "
+                                              "40 GB admission budget) + delta-weighted regression control "
+                                              "variate on every request",
+                   "requests": n_req, "windows": args.steps, "window_s": WINDOW_S, "arrival_rate": RATE,
+                   "l2": "inputs are descriptors; L2 flushed (256 MB write) before the timed stream",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "price": statistics.mean(r[3] for r in res), "rel_halfwidth": rel_err,
-        "path_steps_per_s": path_steps / kernel_s * world,
-        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak_tflops, "unit": "TFLOP/s",
-                     "frac": achieved / fp32_peak_tflops,
-                     "traffic": (traffic["bytes_per_path"] * n_target) if traffic else None,
-                     "kernel": "price_kernel<2,diag>", "kernel_ms": kernel_s * 1e3,
-                     "flops_per_path_step": algorithmic_flops_per_path_step(2),
+        "latency_ms": {"p50": summ["p50_ms"], "p99": summ["p99_ms"], "mean": summ["mean_ms"], "max": summ["max_ms"]},
+        "served": summ,
+        "plain": {"prices_per_s": plain["prices_per_s"], "p50_ms": plain["p50_ms"], "p99_ms": plain["p99_ms"],
+                  "requests": plain["requests"], "windows": b["plain_windows"], "paths": plain["paths"],
+                  "form": "plain run_mc, one request at a time: pilot K1 + readback, main K1 + readback"},
+        "speedup_vs_plain": {"prices_per_s_e2e": e2e / plain["prices_per_s"],
+                             "p50": plain["p50_ms"] / summ["p50_ms"], "p99": plain["p99_ms"] / summ["p99_ms"]},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak, "traffic": None,
+                     "kernel": "serve_kernel (all classes) over the server's device busy time",
+                     "flops": "sum over requests of (pilot + main paths) x (steps + jump rate x T) x F(d)",
                      "peak_source": "measured FFMA probe on this GPU (sdemc_fp32_probe)"},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": ctypes.sizeof(N.SdemcInst),
-                "d2h_bytes_per_step": 48},
-        "gpu_launches": 2 * args.steps,
-        "wall_s": wall,
+        "e2e": {"value": e2e, "unit": UNIT,
+                "h2d_bytes_per_step": b["delta"]["h2d_bytes"] / args.steps,
+                "d2h_bytes_per_step": b["delta"]["d2h_bytes"] / args.steps},
+        "gpu_launches": b["delta"]["launches"],
+        "server": {"ticks": b["delta"]["ticks"], "busy_s": busy, "wall_s": wall},
     }
     if rank == 0:
         line["clocks"] = clk.summary()
-        line["batched_mix"] = bench_batched_mix(args.steps, args.warmup)
-        from sde_mc_gb300.lowering import lower as lw
-
-        def factory(n):
-            return lw(solver, payoff, disc, num_paths=n, path_offset=0, seed=1)
-        pps, n, dt, threads = cpu_sample(factory, n_target, args.cpu_seconds)
-        line["cpu_baseline"] = {"value": pps / n_target, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": "%d paths in %.2f s on %d threads, extrapolated to %d paths per price"
-                                          % (n, dt, threads, n_target)}
+        secs = [s.strip() for s in args.sections.split(",") if s.strip() and s.strip() != "none"]
+        if "c2" in secs:
+            line["c2_plain"] = _section(bench_c2_plain, dev, 20, 5, fp32_peak)
+        if "mlmc" in secs:
+            line["c2_mlmc"] = _section(bench_c2_mlmc, dev)
+        if "mix" in secs:
+            line["batched_mix"] = _section(bench_batched_mix, 5, 3)
+        if "cv" in secs:
+            line["cv_learned"] = _section(bench_cv_learned, dev)
+        spr, n, threads, paths = oracle_serve(b["timed"], args.cpu_seconds)
+        line["cpu_baseline"] = {"value": 1.0 / spr, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": "%d requests of the timed stream (pilot + main, plain estimator, %d paths "
+                                          "simulated) on %d threads; long main runs timed on a prefix of their "
+                                          "paths and extrapolated" % (n, paths, threads)}
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()

@@ -406,7 +406,10 @@ typedef struct {
 typedef struct {
   int64_t submitted, admitted, completed, pending, active;
   int64_t ticks, mem_in_use, mem_peak;
-  int64_t path_steps;       /* executed path-steps (all slices)                 */
+  int64_t path_steps;       /* expected path-steps of all slices (nominal steps
+                               plus expected jumps per path)                   */
+  int64_t launches;         /* kernels launched (install, class, reduce)        */
+  int64_t h2d_bytes, d2h_bytes;  /* plan/slot uploads and phase-record readbacks */
   double busy_s;            /* sum of tick durations on the device              */
 } sdemc_server_stats;
 

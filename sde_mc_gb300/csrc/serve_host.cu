@@ -191,7 +191,7 @@ struct TickBuf {
   unsigned long long* counters_d = nullptr;
   double* part_d = nullptr;
   cudaEvent_t t0 = nullptr, t1 = nullptr;
-  int n_entries = 0, n_installs = 0, n_done = 0;
+  int n_entries = 0, n_installs = 0, n_done = 0, launches = 0;
   double path_steps = 0.0;
 };
 
@@ -477,6 +477,7 @@ int Server::enqueue(TickBuf& B) {
     ++launched;
     k = j;
   }
+  B.launches = launched + 1 + (B.n_entries > 0 ? 1 : 0);
   if (nside > 0) {
     for (int j = 0; j < nside; ++j) {
       if ((rc = check_cuda(cudaEventRecord(join[j], side[j]), "join record"))) return rc;
@@ -530,6 +531,10 @@ int Server::process(TickBuf& B) {
     st.ticks++;
     st.busy_s += ms * 1e-3;
     st.path_steps += (int64_t)B.path_steps;
+    st.launches += B.launches;
+    st.h2d_bytes += (int64_t)B.n_installs * (int64_t)sizeof(ServeInstall) +
+                    (int64_t)B.n_entries * (int64_t)sizeof(ServeEntry);
+    st.d2h_bytes += (int64_t)B.n_done * (int64_t)sizeof(ServeDone);
   }
   for (int i = 0; i < B.n_done; ++i) {
     const ServeDone& R = B.done_h[i];

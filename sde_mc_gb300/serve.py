@@ -11,10 +11,12 @@ the memory budget allow.  A request's slices depend on the request alone, so
 its result is bit-identical whether it ran alone or in any mix.
 
 With ``estimator='linear_cv'`` the pilot also fits, by regression, the
-coefficients of the control variate Y_i = sum_k X^i_k dW^i_k (zero mean under
-the Euler scheme) and the main run prices payoff - beta . Y, which needs
-fewer paths for the same target; the plain estimator stays the fallback when
-the pilot shows no gain.
+coefficients of 2d control variates — per asset, the integrals of w X^i
+against the Brownian increments and against the compensated jump measure,
+with w a Black-Scholes delta of the payoff's underlying; both have mean
+exactly zero under the Euler scheme — and the main run prices payoff -
+beta . r, which needs far fewer paths for the same target.  The plain
+estimator stays the fallback when the pilot shows no gain.
 
 Example::
 
@@ -59,6 +61,7 @@ class ServerStats(ctypes.Structure):
     _fields_ = [("submitted", ctypes.c_int64), ("admitted", ctypes.c_int64), ("completed", ctypes.c_int64),
                 ("pending", ctypes.c_int64), ("active", ctypes.c_int64), ("ticks", ctypes.c_int64),
                 ("mem_in_use", ctypes.c_int64), ("mem_peak", ctypes.c_int64), ("path_steps", ctypes.c_int64),
+                ("launches", ctypes.c_int64), ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64),
                 ("busy_s", ctypes.c_double)]
 
 
