@@ -73,9 +73,11 @@ CvWeights cv_weights(const sdemc_inst& I) {
   CvWeights cw{};
   const int d = I.dim;
   double jump_var = 0.0;
-  if (I.rate > 0.f && I.mark == SDEMC_MARK_LOGNORMAL) {
-    const double a = I.mark_p[0], g = I.mark_p[1];
-    const double kappa = std::exp(a + 0.5 * g * g) - 1.0;
+  const double a = I.mark_p[0], g = I.mark_p[1];
+  const double kappa = std::exp(a + 0.5 * g * g) - 1.0;
+  // the jump regressor is carried divided by its compensator rate, so it
+  // needs E[J] != 0; an asset that never jumps gets rate 0 (regressor 0)
+  if (I.rate > 0.f && I.mark == SDEMC_MARK_LOGNORMAL && std::fabs(kappa) > 1e-9) {
     for (int i = 0; i < d; ++i) {
       double p = 1.0;
       if (I.jump_target == SDEMC_JUMP_ONE_ASSET) {

@@ -97,61 +97,73 @@ struct ServeParams {
 //   r_{d+i} = sum_k w_k X^i_k (J^i_{k+1} - comp_i dt_k)
 // with X_k the state at the start of step k (after the previous step's
 // jump), dW_k the step's correlated increment, J^i_{k+1} the mark applied to
-// asset i at the end of the step (0 without a jump) and w_k = w(t_k, X_k).
-// Both are stochastic integrals of predictable integrands against
+// asset i at the end of the step (0 without a jump) and w_k the weight at the
+// start of the step's 4-step block (w(t_j, X_j), j = 4 floor(k / 4): known at
+// t_k).  Both are stochastic integrals of predictable integrands against
 // martingales (the Brownian increments; the jump measure minus its
 // compensator on the jump-adapted grid), so each has mean exactly zero under
 // the Euler scheme whatever the weights.  Frozen lanes (dt = 0, dW = 0, no
-// jump) add nothing.
+// jump) add nothing.  The jump regressor is carried as a_i with
+// r_{d+i} = -comp_i a_i: every step adds w X dt, a jump subtracts
+// w X J / comp_i (comp_i != 0 whenever jumps are on).
+constexpr int kWeightEvery = 4;
+
 template <int D>
 struct DeltaCvSink {
   static constexpr bool kWantsLeft = false;
   const CvWeights* cw;
-  float xp[D], r[2 * D];
-  float tp;
+  float xp[D], r[D], a[D];
+  float tp, w;
 
   SDEMC_DI float weight() const {
     if (cw->wkind == 0) return 1.f;
-    float a = xp[0];
+    float m = xp[0];
     if (cw->agg == 1) {
 #pragma unroll
-      for (int i = 1; i < D; ++i) a = __fadd_rn(a, xp[i]);
-      a = __fmul_rn(a, 1.f / (float)D);
+      for (int i = 1; i < D; ++i) m = __fadd_rn(m, xp[i]);
+      m = __fmul_rn(m, 1.f / (float)D);
     } else if (cw->agg == 2) {
 #pragma unroll
-      for (int i = 1; i < D; ++i) a = fmaxf(a, xp[i]);
+      for (int i = 1; i < D; ++i) m = fmaxf(m, xp[i]);
     }
-    a = __fmul_rn(a, cw->scale_over_k);
+    m = __fmul_rn(m, cw->scale_over_k);
     const float tau = fmaxf(__fsub_rn(cw->T, tp), 1e-6f);
-    const float d1 = a > 0.f ? __fmul_rn(__fmaf_rn(cw->drift, tau, __logf(a)), __fmul_rn(rsqrtf(tau), cw->inv_sig))
+    const float d1 = m > 0.f ? __fmul_rn(__fmaf_rn(cw->drift, tau, __logf(m)), __fmul_rn(rsqrtf(tau), cw->inv_sig))
                              : -inf_f();
-    const float w = normcdff(d1);
-    return cw->wkind == 2 ? w - 1.f : w;
+    const float v = normcdff(d1);
+    return cw->wkind == 2 ? v - 1.f : v;
   }
 
   template <int DD> SDEMC_DI void init(const float* x) {
 #pragma unroll
-    for (int i = 0; i < D; ++i) { xp[i] = x[i]; r[i] = 0.f; r[D + i] = 0.f; }
+    for (int i = 0; i < D; ++i) { xp[i] = x[i]; r[i] = 0.f; a[i] = 0.f; }
     tp = 0.f;
+    w = weight();
   }
   template <int DD, int NW>
-  SDEMC_DI void step(int, const float*, const float* x, float t, float J, int sel, const float* dW, const float*,
+  SDEMC_DI void step(int k, const float*, const float* x, float t, float J, int sel, const float* dW, const float*,
                      const float*, int jump_one) {
-    const float w = weight();
-    const float dt = __fsub_rn(t, tp);
+    if (k > 0 && (k & (kWeightEvery - 1)) == 0) w = weight();  // k is warp-uniform
 #pragma unroll
-    for (int i = 0; i < D; ++i) {
-      const float wx = __fmul_rn(w, xp[i]);
-      r[i] = __fmaf_rn(wx, dW[i], r[i]);
-      if (cw->jumps) {
-        const float ji = (jump_one && i != sel) ? 0.f : J;
-        r[D + i] = __fmaf_rn(wx, __fmaf_rn(-cw->comp[i], dt, ji), r[D + i]);
+    for (int i = 0; i < D; ++i) r[i] = __fmaf_rn(xp[i], __fmul_rn(w, dW[i]), r[i]);
+    if (cw->jumps) {
+      const float wdt = __fmul_rn(w, __fsub_rn(t, tp));
+#pragma unroll
+      for (int i = 0; i < D; ++i) a[i] = __fmaf_rn(xp[i], wdt, a[i]);
+      if (J != 0.f) {
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+          if (!jump_one || i == sel) a[i] = __fmaf_rn(-__fmul_rn(w, xp[i]), __fdividef(J, cw->comp[i]), a[i]);
       }
-      xp[i] = x[i];
     }
+#pragma unroll
+    for (int i = 0; i < D; ++i) xp[i] = x[i];
     tp = t;
   }
   template <int DD, int NW> SDEMC_DI void finish(int, const float*, float) {}
+
+  // Regressor q (0 <= q < 2D).
+  SDEMC_DI float reg(int q) const { return q < D ? r[q] : -__fmul_rn(cw->comp[q - D], a[q - D]); }
 };
 
 template <int D, int NOISE, int MODE, int KIND>
@@ -225,7 +237,7 @@ serve_kernel(const __grid_constant__ ServeParams P) {
       const float pv = valid ? __fmul_rn(payoff<D>(I, x), I.discount) : 0.f;
       float y[R];
 #pragma unroll
-      for (int i = 0; i < R; ++i) y[i] = valid ? sk.r[i] : 0.f;
+      for (int i = 0; i < R; ++i) y[i] = valid ? sk.reg(i) : 0.f;
       if (KIND == kKindLcv) {
         float v = pv;
 #pragma unroll
