@@ -47,6 +47,13 @@ struct SeedKeys {
   uint32_t k0, k1;
   SDEMC_DI uint32_t a(int r) const { return k0 + (uint32_t)r * 0x9E3779B9u; }
   SDEMC_DI uint32_t b(int r) const { return k1 + (uint32_t)r * 0xBB67AE85u; }
+  // A copy whose schedule the compiler must derive again at each use, so the
+  // 20 round keys are not held live across a whole path loop.
+  SDEMC_DI SeedKeys fresh() const {
+    SeedKeys c = *this;
+    asm volatile("" : "+r"(c.k0), "+r"(c.k1));
+    return c;
+  }
 };
 struct ConstKeys {
   const RoundKeys* rk;
@@ -55,7 +62,12 @@ struct ConstKeys {
 };
 
 template <class KS>
-SDEMC_DI U4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, const KS& ks) {
+SDEMC_DI const KS& fresh_keys(const KS& ks) { return ks; }
+SDEMC_DI SeedKeys fresh_keys(const SeedKeys& ks) { return ks.fresh(); }
+
+template <class KS>
+SDEMC_DI U4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, const KS& ks_in) {
+  const auto ks = fresh_keys(ks_in);
 #pragma unroll
   for (int r = 0; r < 10; ++r) {
     const uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
