@@ -429,6 +429,7 @@ def bench_cv_learned(dev, epochs=10):
     dl = sm.simulate_adapted_data(1 << 18, solver, payoff, disc, bs=4096)
     torch.cuda.synchronize()
     t_sim = time.perf_counter() - t0
+    train_steps = int(dl.dataset.normals.shape[1])
     t0 = time.perf_counter()
     losses = sm.train_adapted_control_variates(models, opt, dl, solver, disc, epochs=epochs, print_losses=False)
     torch.cuda.synchronize()
@@ -440,28 +441,59 @@ def bench_cv_learned(dev, epochs=10):
     st_cv = sm.mc_apply_cvs(models, solver, n_eval, payoff, disc, sim_bs=1 << 18, bs=4096)
     torch.cuda.synchronize()
     t_eval = time.perf_counter() - t0
+    eval_steps = train_steps  # same model and grid: the adapted step count per batch
     plain = sm.price_stats(solver, payoff, disc, n_eval, payoff_time='adapted', path_offset=start)
     mean_p, se_p, _ = sm.finish_stats(plain)
     vrf = (se_p / st_cv.sample_std) ** 2
     bias = st_cv.sample_mean - mean_p
+    # tensor-core work: K5 forward 2(3*64 + 64*64 + 64*64 + 64*2) flops per
+    # (path, step) row; a training step runs K5 and K6 (forward recompute,
+    # input and weight gradients: three forwards' worth)
+    fwd = 2 * (3 * 64 + 64 * 64 + 64 * 64 + 64 * 2)
+    rows_train = epochs * ((1 << 18) // 4096) * 4096 * train_steps
+    rows_eval = n_eval * eval_steps
+    peaks = load_json_file("MEASURED_PEAKS.json") or {}
+    bf16 = peaks.get("bf16_tflops")
+    tf_train = rows_train * 4 * fwd / t_train / 1e12
+    tf_eval = rows_eval * fwd / t_eval / 1e12
+    # the served form's regression control variate on the same model and target
+    from sde_mc_gb300 import serve
+    with serve.Server(max_slots=8, mem_budget=1 << 30, device=dev) as srv:
+        for tag, est in ((1, "plain"), (2, "linear_cv")):
+            srv.submit(solver, payoff, disc, rel_target=1e-3, pilot_paths=1 << 18, estimator=est, tag=tag,
+                       stream_id=1000)
+        reg = {r.tag: r for r in srv.wait(2)}
     return {"workload": "config-4 learned CV on the config-2 model, Mlp(3,[64,64,64],2) ReLU no BN, Adam lr 1e-3 "
                         "batch 4096, %d epochs on 2^18 solver paths, evaluated on 2^22 fresh paths" % epochs,
             "vrf": vrf, "mean_cv": st_cv.sample_mean, "se_cv": st_cv.sample_std, "mean_plain": mean_p,
             "se_plain": se_p, "bias": bias, "bias_in_se": bias / math.hypot(st_cv.sample_std, se_p),
             "loss_first_last": [losses[0], losses[-1]], "simulate_s": t_sim, "train_s": t_train, "eval_s": t_eval,
-            "note": "the plain estimate uses the same 2^22 fresh paths as the control-variate estimate"}
+            "train_rows": rows_train, "eval_rows": rows_eval,
+            "train_tflops": tf_train, "eval_tflops_incl_paths": tf_eval,
+            "bf16_peak_tflops": bf16, "train_frac_of_bf16_peak": (tf_train / bf16) if bf16 else None,
+            "regression_cv_same_model": {"vrf": reg[2].vrf, "mean": reg[2].mean, "se": reg[2].se,
+                                         "plain_mean": reg[1].mean, "plain_se": reg[1].se,
+                                         "main_paths_cv": reg[2].main_paths, "main_paths_plain": reg[1].main_paths},
+            "note": "the plain estimate uses the same 2^22 fresh paths as the control-variate estimate; eval time "
+                    "includes materialising the paths (K4)"}
 
 
-def bench_served(dev, steps, warmup, plain_windows):
+def shard(reqs, rank, world):
+    """Requests of one rank: the stream is partitioned by request index (each
+    request is independent; no exchange on the data path)."""
+    return [r for r in reqs if r.idx % world == rank]
+
+
+def bench_served(dev, steps, warmup, plain_windows, rank=0, world=1):
     """The headline: K windows of the served stream through the server, and
     the plain one-request-per-launch server on the first windows."""
     import torch
     from sde_mc_gb300 import serve
     from sde_mc_gb300 import stream as S
     srv = serve.Server(max_slots=4096, mem_budget=40 << 30, side_streams=4, policy="srpt", device=dev)
-    warm = stream_windows(0, warmup)
+    warm = shard(stream_windows(0, warmup), rank, world)
     S.run_served(warm, srv)
-    timed = stream_windows(warmup, steps)
+    timed = shard(stream_windows(warmup, steps), rank, world)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     flush.fill_(1)
     torch.cuda.synchronize()
@@ -533,7 +565,7 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        b = bench_served(dev, args.steps, args.warmup, args.plain_windows)
+        b = bench_served(dev, args.steps, args.warmup, args.plain_windows, rank, world)
     if world > 1:
         dist.barrier()
     summ, busy = b["summary"], b["busy_s"]
@@ -543,20 +575,24 @@ def main():
         t = torch.tensor([busy, wall], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         busy, wall = float(t[0]), float(t[1])
-    value = world * n_req / busy
-    e2e = world * n_req / wall
+        c = torch.tensor([n_req], device=dev, dtype=torch.float64)
+        dist.all_reduce(c, op=dist.ReduceOp.SUM)
+        n_req = int(c.item())
+    value = n_req / busy
+    e2e = n_req / wall
     achieved = b["flops"] / busy / 1e12
     plain = b["plain"]
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": busy * 1e3 / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "scaling": "strong", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "form": "served: continuous-batching server (SRPT ticks, 4 side streams, "
                                               "40 GB admission budget) + delta-weighted regression control "
                                               "variate on every request",
                    "requests": n_req, "windows": args.steps, "window_s": WINDOW_S, "arrival_rate": RATE,
                    "l2": "inputs are descriptors; L2 flushed (256 MB write) before the timed stream",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+                   "parallelism": ("stream sharded by request index over %d GPUs" % world) if world > 1
+                   else "single GPU"},
         "latency_ms": {"p50": summ["p50_ms"], "p99": summ["p99_ms"], "mean": summ["mean_ms"], "max": summ["max_ms"]},
         "served": summ,
         "plain": {"prices_per_s": plain["prices_per_s"], "p50_ms": plain["p50_ms"], "p99_ms": plain["p99_ms"],

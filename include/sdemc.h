@@ -355,11 +355,12 @@ int sdemc_adam_step(float* d_params, const float* d_grad, float* d_m, float* d_v
  * bits whether the request ran alone or in any mix.
  *
  * Estimators: SDEMC_EST_PLAIN is the reference's plain estimator.
- * SDEMC_EST_LINEAR_CV adds 2d control variates, per asset i
+ * SDEMC_EST_LINEAR_CV adds 2d + 1 control variates, per asset i
  *   sum_k w_k X^i_k dW^i_k  and  sum_k w_k X^i_k (J^i_{k+1} - lambda_i E[J] dt_k),
- * stochastic integrals against the Brownian increments and the compensated
- * jump measure of the jump-adapted grid (mean exactly zero under the Euler
- * scheme), with w_k a Black-Scholes delta of the payoff's underlying; their
+ * and sum_k g_k (J_{k+1}^2 - lambda E[J^2] dt_k): stochastic integrals against
+ * the Brownian increments and the compensated jump measures of the
+ * jump-adapted grid (mean exactly zero under the Euler scheme), with w_k a
+ * Black-Scholes delta and g_k a scaled gamma of the payoff's underlying; their
  * coefficients are fitted by regression on the pilot and the main run prices
  * payoff - beta . r on fresh paths, so it stays unbiased.  Jump terms are on
  * for lognormal marks (E[J] known exactly).  When the pilot shows no variance
@@ -400,7 +401,8 @@ typedef struct {
   double vrf;               /* pilot variance / control-variate residual var.   */
   int64_t pilot_paths, main_paths;
   int64_t t_arrive_ns, t_admit_ns, t_done_ns;  /* CLOCK_MONOTONIC               */
-  float beta[2 * SDEMC_MAX_DIM];  /* control-variate coefficients (Brownian, jump) */
+  float beta[2 * SDEMC_MAX_DIM + 1];  /* control-variate coefficients     */
+  float reserved1;
 } sdemc_result;
 
 typedef struct {

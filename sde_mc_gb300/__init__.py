@@ -14,3 +14,4 @@ from .mc import *
 from .mlmc import *
 from .nets import *
 from .varred import *
+from . import torch_ops  # registers torch.ops.sdemc.*

@@ -87,6 +87,8 @@ CvWeights cv_weights(const sdemc_inst& I) {
       cw.comp[i] = (float)((double)I.rate * p * kappa);
     }
     cw.jumps = 1;
+    // E[J^2] for J = exp(N(a, g^2)) - 1
+    cw.comp_j2 = (float)((double)I.rate * (std::exp(2.0 * a + 2.0 * g * g) - 2.0 * std::exp(a + 0.5 * g * g) + 1.0));
     jump_var = (double)I.rate * (a * a + g * g) / (I.jump_target == SDEMC_JUMP_ONE_ASSET ? d : 1);
   }
   switch (I.payoff) {
@@ -562,7 +564,7 @@ int Server::process(TickBuf& B) {
     h.vrf = 1.0;
     for (int k = 0; k < kServeMaxR; ++k) h.beta[k] = 0.f;
     if (h.kind == kKindPilotStats && n > 2) {
-      const int nr = 2 * h.req.inst.dim;
+      const int nr = num_regressors(h.req.inst.dim);
       double ybar[kServeMaxR], C[kServeMaxR * kServeMaxR], c[kServeMaxR], beta[kServeMaxR];
       for (int a = 0; a < nr; ++a) ybar[a] = R.acc[3 + a] / n;
       int q = 3 + nr;

@@ -23,29 +23,36 @@
 
 namespace sdemc {
 
-constexpr int kServeMaxR = 2 * SDEMC_MAX_DIM;  // control-variate regressors
-constexpr int kServeMaxW = 3 + 2 * kServeMaxR + kServeMaxR * (kServeMaxR + 1) / 2;  // 171
+constexpr int kServeMaxR = 2 * SDEMC_MAX_DIM + 1;  // control-variate regressors
+constexpr int kServeMaxW = 3 + 2 * kServeMaxR + kServeMaxR * (kServeMaxR + 1) / 2;  // 190
 constexpr int kServeMaxWarps = 8;  // CTAs of up to 256 threads
 enum { kKindPlain = 0, kKindLcv = 1, kKindPilotStats = 2, kNumKinds = 3 };
 
-// Pilot partial layout over the R = 2d regressors r (see DeltaCvSink):
+// Pilot partial layout over the R = 2d + 1 regressors r (see DeltaCvSink):
 // P, P^2, n, r[R], r_a r_b (a <= b, row-major), P r[R].
-SDEMC_HDI int pilot_width(int d) { return 3 + 4 * d + d * (2 * d + 1); }
+SDEMC_HDI int num_regressors(int d) { return 2 * d + 1; }
+SDEMC_HDI int pilot_width(int d) {
+  const int R = num_regressors(d);
+  return 3 + 2 * R + R * (R + 1) / 2;
+}
 SDEMC_HDI int kind_width(int kind, int d) { return kind == kKindPilotStats ? pilot_width(d) : 3; }
 
-// Integrand weight of the control variate: w(t, X) = N(d1) (call-like
+// Integrand weights of the control variate: w(t, X) = N(d1) (call-like
 // payoffs) or N(d1) - 1 (puts) of a lognormal proxy of the payoff's
 // underlying A = payoff_scale * agg(X) (asset 0, mean or max): d1 =
 // (ln(A/K) + drift tau) / (sig sqrt(tau)), tau = T - t; w = 1 when
-// wkind == 0.  Any deterministic weight keeps the control variate unbiased;
-// this one makes it close to a delta hedge.  comp[i]
-// is the jump compensator rate lambda_i E[J] of asset i; jump regressors are
-// on only when that rate is known exactly (lognormal marks).
+// wkind == 0 — a delta; and g(t, X) = (A/K) phi(d1) / (sig sqrt(tau)) (g = 1
+// when wkind == 0) — a gamma scaled by A^2/K.  Any deterministic weights keep
+// the control variate unbiased; these make it close to a delta hedge plus the
+// second-order jump exposure.  comp[i] is the jump compensator rate
+// lambda_i E[J] of asset i and comp_j2 = lambda E[J^2]; jump regressors are on
+// only when those rates are known exactly (lognormal marks).
 struct CvWeights {
   float comp[SDEMC_MAX_DIM];
   float scale_over_k;  // payoff_scale / K
   float inv_sig, drift, T;
-  int32_t agg, wkind, jumps, pad;
+  float comp_j2;
+  int32_t agg, wkind, jumps;
 };
 
 struct ServeState {
@@ -95,17 +102,20 @@ struct ServeParams {
 // The control variate's regressors, per asset i:
 //   r_i     = sum_k w_k X^i_k dW^i_k
 //   r_{d+i} = sum_k w_k X^i_k (J^i_{k+1} - comp_i dt_k)
+// and one more,
+//   r_{2d}  = sum_k g_k (J_{k+1}^2 - comp_j2 dt_k),
 // with X_k the state at the start of step k (after the previous step's
-// jump), dW_k the step's correlated increment, J^i_{k+1} the mark applied to
-// asset i at the end of the step (0 without a jump) and w_k the weight at the
-// start of the step's 4-step block (w(t_j, X_j), j = 4 floor(k / 4): known at
-// t_k).  Both are stochastic integrals of predictable integrands against
-// martingales (the Brownian increments; the jump measure minus its
-// compensator on the jump-adapted grid), so each has mean exactly zero under
+// jump), dW_k the step's correlated increment, J_{k+1} the mark of a jump at
+// the end of the step (J^i_{k+1} the part applied to asset i; 0 without a
+// jump) and (w_k, g_k) the weights at the start of the step's 4-step block
+// (evaluated at t_j, X_j, j = 4 floor(k / 4): known at t_k).  All are
+// stochastic integrals of predictable integrands against martingales (the
+// Brownian increments; the jump measures of J and J^2 minus their
+// compensators on the jump-adapted grid), so each has mean exactly zero under
 // the Euler scheme whatever the weights.  Frozen lanes (dt = 0, dW = 0, no
-// jump) add nothing.  The jump regressor is carried as a_i with
-// r_{d+i} = -comp_i a_i: every step adds w X dt, a jump subtracts
-// w X J / comp_i (comp_i != 0 whenever jumps are on).
+// jump) add nothing.  A jump regressor is carried as a with r = -comp a:
+// every step adds weight x dt, a jump subtracts weight x J / comp (the
+// compensator rates are nonzero whenever jumps are on).
 constexpr int kWeightEvery = 4;
 
 template <int D>
@@ -113,10 +123,10 @@ struct DeltaCvSink {
   static constexpr bool kWantsLeft = false;
   const CvWeights* cw;
   float xp[D], r[D], a[D];
-  float tp, w;
+  float tp, w, g, ag;
 
-  SDEMC_DI float weight() const {
-    if (cw->wkind == 0) return 1.f;
+  SDEMC_DI void weights() {
+    if (cw->wkind == 0) { w = 1.f; g = 1.f; return; }
     float m = xp[0];
     if (cw->agg == 1) {
 #pragma unroll
@@ -128,32 +138,42 @@ struct DeltaCvSink {
     }
     m = __fmul_rn(m, cw->scale_over_k);
     const float tau = fmaxf(__fsub_rn(cw->T, tp), 1e-6f);
-    const float d1 = m > 0.f ? __fmul_rn(__fmaf_rn(cw->drift, tau, __logf(m)), __fmul_rn(rsqrtf(tau), cw->inv_sig))
-                             : -inf_f();
-    const float v = normcdff(d1);
-    return cw->wkind == 2 ? v - 1.f : v;
+    const float is = __fmul_rn(rsqrtf(tau), cw->inv_sig);
+    if (m > 0.f) {
+      const float d1 = __fmul_rn(__fmaf_rn(cw->drift, tau, __logf(m)), is);
+      const float v = normcdff(d1);
+      w = cw->wkind == 2 ? v - 1.f : v;
+      g = __fmul_rn(__fmul_rn(m, is), __fmul_rn(0.39894228f, __expf(__fmul_rn(-0.5f, __fmul_rn(d1, d1)))));
+    } else {
+      w = cw->wkind == 2 ? -1.f : 0.f;
+      g = 0.f;
+    }
   }
 
   template <int DD> SDEMC_DI void init(const float* x) {
 #pragma unroll
     for (int i = 0; i < D; ++i) { xp[i] = x[i]; r[i] = 0.f; a[i] = 0.f; }
     tp = 0.f;
-    w = weight();
+    ag = 0.f;
+    weights();
   }
   template <int DD, int NW>
   SDEMC_DI void step(int k, const float*, const float* x, float t, float J, int sel, const float* dW, const float*,
                      const float*, int jump_one) {
-    if (k > 0 && (k & (kWeightEvery - 1)) == 0) w = weight();  // k is warp-uniform
+    if (k > 0 && (k & (kWeightEvery - 1)) == 0) weights();  // k is warp-uniform
 #pragma unroll
     for (int i = 0; i < D; ++i) r[i] = __fmaf_rn(xp[i], __fmul_rn(w, dW[i]), r[i]);
     if (cw->jumps) {
-      const float wdt = __fmul_rn(w, __fsub_rn(t, tp));
+      const float dt = __fsub_rn(t, tp);
+      const float wdt = __fmul_rn(w, dt);
 #pragma unroll
       for (int i = 0; i < D; ++i) a[i] = __fmaf_rn(xp[i], wdt, a[i]);
+      ag = __fmaf_rn(g, dt, ag);
       if (J != 0.f) {
 #pragma unroll
         for (int i = 0; i < D; ++i)
           if (!jump_one || i == sel) a[i] = __fmaf_rn(-__fmul_rn(w, xp[i]), __fdividef(J, cw->comp[i]), a[i]);
+        ag = __fmaf_rn(-g, __fdividef(__fmul_rn(J, J), cw->comp_j2), ag);
       }
     }
 #pragma unroll
@@ -162,22 +182,26 @@ struct DeltaCvSink {
   }
   template <int DD, int NW> SDEMC_DI void finish(int, const float*, float) {}
 
-  // Regressor q (0 <= q < 2D).
-  SDEMC_DI float reg(int q) const { return q < D ? r[q] : -__fmul_rn(cw->comp[q - D], a[q - D]); }
+  // Regressor q (0 <= q < 2D + 1).
+  SDEMC_DI float reg(int q) const {
+    if (q < D) return r[q];
+    if (q < 2 * D) return -__fmul_rn(cw->comp[q - D], a[q - D]);
+    return -__fmul_rn(cw->comp_j2, ag);
+  }
 };
 
 template <int D, int NOISE, int MODE, int KIND>
 __global__ void __launch_bounds__(256)
 serve_kernel(const __grid_constant__ ServeParams P) {
   __shared__ sdemc_inst s_inst[kServeMaxWarps];
-  __shared__ float s_beta[kServeMaxWarps][2 * D];
+  __shared__ float s_beta[kServeMaxWarps][2 * D + 1];
   __shared__ CvWeights s_cw[kServeMaxWarps];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int slot = -1;
   int64_t lo = 0, hi = 0, base = 0, end = 0, part_off = 0;
   int max_iters = 0;
   bool ovf = false;
-  constexpr int R = 2 * D;
+  constexpr int R = 2 * D + 1;
   constexpr int W = KIND == kKindPilotStats ? 3 + 2 * R + R * (R + 1) / 2 : 3;
   for (;;) {
     unsigned long long g = 0;

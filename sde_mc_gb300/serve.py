@@ -11,10 +11,11 @@ the memory budget allow.  A request's slices depend on the request alone, so
 its result is bit-identical whether it ran alone or in any mix.
 
 With ``estimator='linear_cv'`` the pilot also fits, by regression, the
-coefficients of 2d control variates — per asset, the integrals of w X^i
+coefficients of 2d + 1 control variates — per asset, the integrals of w X^i
 against the Brownian increments and against the compensated jump measure,
-with w a Black-Scholes delta of the payoff's underlying; both have mean
-exactly zero under the Euler scheme — and the main run prices payoff -
+with w a Black-Scholes delta of the payoff's underlying, and the integral of
+a gamma weight against the compensated measure of squared jumps; all have
+mean exactly zero under the Euler scheme — and the main run prices payoff -
 beta . r, which needs far fewer paths for the same target.  The plain
 estimator stays the fallback when the pilot shows no gain.
 
@@ -54,7 +55,8 @@ class Result(ctypes.Structure):
                 ("mean", ctypes.c_double), ("se", ctypes.c_double), ("pilot_mean", ctypes.c_double),
                 ("pilot_se", ctypes.c_double), ("vrf", ctypes.c_double), ("pilot_paths", ctypes.c_int64),
                 ("main_paths", ctypes.c_int64), ("t_arrive_ns", ctypes.c_int64), ("t_admit_ns", ctypes.c_int64),
-                ("t_done_ns", ctypes.c_int64), ("beta", ctypes.c_float * (2 * N.MAX_DIM))]
+                ("t_done_ns", ctypes.c_int64), ("beta", ctypes.c_float * (2 * N.MAX_DIM + 1)),
+                ("reserved1", ctypes.c_float)]
 
 
 class ServerStats(ctypes.Structure):

@@ -242,3 +242,18 @@ def test_basket_mix_law():
     assert 2 ** 12 <= min(paths) and max(paths) <= 2 ** 18
     assert all(0.8 <= m.payoff.strike <= 1.2 for m in mix)
     assert [m.stream_id for m in mix] == list(range(512))
+
+
+def test_torch_ops_registered_with_schemas():
+    """Every C-ABI compute entry point the estimators use is a torch op with a
+    typed schema (registration needs no GPU)."""
+    from sde_mc_gb300 import torch_ops
+    for name in torch_ops.OPS:
+        op = getattr(torch.ops.sdemc, name)
+        assert str(op.default._schema).startswith("sdemc::" + name + "(")
+    assert "Tensor(a0!) params" in str(torch.ops.sdemc.adam_step.default._schema)
+    solver, payoff, disc = merton1d()
+    t = torch_ops.inst_tensor(lower(solver, payoff, disc, num_paths=64))
+    assert t.dtype == torch.uint8 and t.numel() == N.load().sdemc_inst_size()
+    with pytest.raises(ValueError):
+        torch_ops._inst(t[:-1])
