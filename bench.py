@@ -312,7 +312,7 @@ def bench_c2_plain(dev, steps, warmup, fp32_peak):
             e2e.append(time.perf_counter() - t0)
     kernel_s = statistics.mean(k_ms) * 1e-3
     achieved = flops / kernel_s / 1e12
-    traffic = load_json_file(os.path.join("profiles", "price_kernel_traffic.json"))
+    traffic = (load_json_file(os.path.join("profiles", "kernel_traffic.json")) or {}).get("price_kernel<2,diag>")
     return {"workload": C2_WORKLOAD, "paths_per_price": n_target, "steps_per_path": steps_per_path,
             "prices_per_s": steps / (sum(k_ms) + sum(r_ms)) * 1e3, "ms_per_price": statistics.mean(
                 [a + b for a, b in zip(k_ms, r_ms)]),
@@ -321,7 +321,9 @@ def bench_c2_plain(dev, steps, warmup, fp32_peak):
             "path_steps_per_s": n_target * steps_per_path / kernel_s,
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                          "frac": achieved / fp32_peak,
-                         "traffic": (traffic["bytes_per_path"] * n_target) if traffic else None,
+                         "traffic": traffic["dram_bytes"] if traffic else None,
+                         "traffic_note": "DRAM bytes of one ncu-captured launch (2^20 paths): descriptor and "
+                                         "chunk partials only; paths stay in registers",
                          "kernel": "price_kernel<2,diag>", "kernel_ms": kernel_s * 1e3,
                          "flops_per_path_step": algorithmic_flops_per_path_step(2),
                          "peak_source": "measured FFMA probe on this GPU (sdemc_fp32_probe)"},
@@ -424,6 +426,7 @@ def bench_cv_learned(dev, epochs=10):
     f = sm.Mlp(3, [64, 64, 64], 2, batch_norm=False, batch_norm_init=False)
     opt = torch.optim.Adam(f.parameters(), lr=1e-3)
     models = [f, sm.ZeroFunction(2)]
+    sm.simulate_adapted_data(1 << 18, solver, payoff, disc, bs=4096)  # warm-up: allocator, first launches
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     dl = sm.simulate_adapted_data(1 << 18, solver, payoff, disc, bs=4096)
@@ -507,11 +510,23 @@ def bench_served(dev, steps, warmup, plain_windows, rank=0, world=1):
     for r in timed:
         x = res[r.idx]
         flops += (x.pilot_paths + x.main_paths) * r.path_steps * algorithmic_flops_per_path_step(r.dim)
+    # capacity: the same requests released at once (no arrival gaps)
+    import copy
+    burst = [copy.copy(r) for r in timed]
+    for r in burst:
+        r.t = 0.0
+    srv = serve.Server(max_slots=4096, mem_budget=40 << 30, side_streams=4, policy="srpt", device=dev)
+    c0 = srv.stats()
+    _, csumm = S.run_served(burst, srv)
+    c1 = srv.stats()
+    srv.close()
+    capacity = {"requests": csumm["requests"], "prices_per_s_busy": csumm["requests"] / (c1["busy_s"] - c0["busy_s"]),
+                "prices_per_s_e2e": csumm["prices_per_s"], "p50_ms": csumm["p50_ms"], "p99_ms": csumm["p99_ms"]}
     plain_reqs = [r for r in timed if r.t < min(steps, plain_windows) * WINDOW_S]
     S.run_plain(warm[:50])
     _, psumm = S.run_plain(plain_reqs)
     # price agreement between the two servers (each within its own error)
-    return {"summary": summ, "busy_s": busy, "delta": delta, "flops": flops, "plain": psumm,
+    return {"summary": summ, "busy_s": busy, "delta": delta, "flops": flops, "plain": psumm, "capacity": capacity,
             "plain_windows": min(steps, plain_windows), "results": res, "timed": timed}
 
 
@@ -598,10 +613,15 @@ def main():
         "plain": {"prices_per_s": plain["prices_per_s"], "p50_ms": plain["p50_ms"], "p99_ms": plain["p99_ms"],
                   "requests": plain["requests"], "windows": b["plain_windows"], "paths": plain["paths"],
                   "form": "plain run_mc, one request at a time: pilot K1 + readback, main K1 + readback"},
+        "served_capacity": dict(b["capacity"], form="the timed requests released at once (no arrival gaps)"),
         "speedup_vs_plain": {"prices_per_s_e2e": e2e / plain["prices_per_s"],
                              "p50": plain["p50_ms"] / summ["p50_ms"], "p99": plain["p99_ms"] / summ["p99_ms"]},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": achieved / fp32_peak, "traffic": None,
+                     "frac": achieved / fp32_peak,
+                     "traffic": ((load_json_file(os.path.join("profiles", "kernel_traffic.json")) or {})
+                                 .get("serve_kernel<6,0,0,1>") or {}).get("dram_bytes"),
+                     "traffic_note": "DRAM bytes of one ncu-captured serve_kernel launch (d = 6 main run): slot "
+                                     "state and chunk partials only; paths stay in registers",
                      "kernel": "serve_kernel (all classes) over the server's device busy time",
                      "flops": "sum over requests of (pilot + main paths) x (steps + jump rate x T) x F(d)",
                      "peak_source": "measured FFMA probe on this GPU (sdemc_fp32_probe)"},
