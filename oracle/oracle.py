@@ -342,3 +342,34 @@ def cv_grads_mixed(params, time, paths, normals, gamma, r):
     inp = np.concatenate([np.asarray(t, np.float64)[:, None], np.asarray(xin, np.float64)], axis=1)
     gW1, gb1 = dz1.T @ inp, dz1.sum(0)
     return [gW1, gb1, gW2, gb2, gW3, gb3, gW4, gb4]
+
+
+def cv_jump_multipliers(time, jumps, lam_kappa):
+    """Per-row multipliers of the jump integrand g in the reference's adapted
+    control variate (sde_mc/varred.py:118-128): the recorded mark J_k minus the
+    compensator lambda E[J] h_k with h = diff(time) — the last row has no
+    compensator because the reference sums g[:, :-1] against diff(time).
+    time (n, S), jumps (n, S, d), lam_kappa scalar or (d,)."""
+    t = np.asarray(time, np.float64)
+    m = np.array(jumps, np.float64, copy=True)
+    h = np.diff(t, axis=1)
+    m[:, :-1, :] -= np.asarray(lam_kappa, np.float64) * h[..., None]
+    return m
+
+
+def cv2_loss_and_grads(pf, pg, time, paths, left, normals, mult_g, payoffs, r):
+    """Var(Gamma) with Gamma = payoff + sum e^{-rt} f(t, X) . dW
+    + sum e^{-rt} g(t, X-) . mult_g, and both networks' gradients (FP64)."""
+    n, S, d = normals.shape
+    t = np.asarray(time, np.float64).reshape(n, S)
+    fin = np.concatenate([t.reshape(-1, 1), np.asarray(paths, np.float64).reshape(-1, d)], 1)
+    gin = np.concatenate([t.reshape(-1, 1), np.asarray(left, np.float64).reshape(-1, d)], 1)
+    disc = np.exp(-t * r)[..., None]
+    fo = mlp_forward(pf, fin)[0].reshape(n, S, d)
+    go = mlp_forward(pg, gin)[0].reshape(n, S, d)
+    a_f = (np.asarray(normals, np.float64) * fo * disc).sum((1, 2))
+    a_g = (mult_g * go * disc).sum((1, 2))
+    pay = np.asarray(payoffs, np.float64)
+    loss, gamma, gf = cv_loss_and_grads(pf, fin, np.asarray(normals, np.float64), t, pay + a_g, r)
+    _, _, gg = cv_loss_and_grads(pg, gin, mult_g, t, pay + a_f, r)
+    return loss, gamma, gf, gg

@@ -1,13 +1,16 @@
 """Learned control variates with the reference's interface (sde_mc/varred.py).
 
-The Brownian integrand f of the adapted control variate
+The adapted control variate (sde_mc/varred.py:98-199)
     Gamma = payoff + sum_k e^{-r t_k} f(t_k, X_k) . dW_k
+                   + sum_k e^{-r t_k} g(t_k, X_k-) . (J_k - lambda E[J] h_k)
 is trained and evaluated on the GPU by the library's kernels (K5/K6): BF16
 tensor-core forward and backward passes with FP32 accumulation, a
 deterministic gradient reduction and a fused Adam step, all on paths the
-solver itself generated.  Training and inference run when the models are
-(``Mlp`` of the supported shape, ``ZeroFunction``) — the jump integrand g is
-not implemented and raises ``NotImplementedError``.
+solver itself generated.  Each network is one kernel pass over its own
+(inputs, multipliers): f reads the path and the Brownian increments, g the
+left limits and the recorded marks minus their compensator (the last row has
+none, as in the reference).  Supported models: ``Mlp(1+d, [64, 64, 64], d)``
+(ReLU, no batch norm, d in {1, 2}) for f and g, ``ZeroFunction`` for g.
 """
 import math
 import time
@@ -68,6 +71,7 @@ class CvData:
 
     @classmethod
     def from_dataset(cls, ds, solver, device):
+        """Inputs of the Brownian integrand f."""
         if hasattr(ds, "full_time"):  # AdaptedPathData
             return cls(ds.full_time.reshape(ds.full_time.shape[0], -1), ds.full_paths, ds.normals, ds.payoffs, device)
         # NormalPathData (uniform grid): times from partition(T, steps, 'left')
@@ -76,20 +80,43 @@ class CvData:
         row = torch.cat([tp, torch.tensor([float(solver.time_interval)])]).to(torch.float32)
         return cls(row.unsqueeze(0).expand(n, steps + 1), ds.full_paths, ds.normals, ds.payoffs, device)
 
+    @classmethod
+    def jumps_from_dataset(cls, ds, solver, device):
+        """Inputs of the jump integrand g (AdaptedPathData): left limits, and
+        per row the recorded marks minus lambda E[J] h_k with h = diff(time)
+        (sde_mc/varred.py:118-128); no payoff term."""
+        if not hasattr(ds, "jump_paths"):
+            raise ValueError("the jump integrand needs AdaptedPathData")
+        n, S, d = ds.normals.shape
+        t = ds.time_paths.reshape(n, S).to(device=device, dtype=torch.float32)
+        lam_kappa = torch.as_tensor(solver.sde.jump_rate() * solver.sde.jump_mean(), dtype=torch.float32,
+                                    device=device)
+        mult = ds.jump_paths.to(device=device, dtype=torch.float32).clone()
+        mult[:, :-1, :] -= lam_kappa * torch.diff(t, dim=1).unsqueeze(-1)
+        left = ds.left_paths.to(device=device, dtype=torch.float32)
+        left_full = torch.cat([left, left[:, -1:]], 1)  # the kernels read rows 0..S-1 of (S+1)
+        return cls(ds.full_time.reshape(n, -1), left_full, mult, torch.zeros(n, device=device), device)
 
-def kernel_models(models):
-    """(f, dim) when (f, g) are a supported Mlp and ZeroFunction, else raise."""
-    if isinstance(models, (list, tuple)):
-        f, g = models
-        if not isinstance(g, ZeroFunction):
-            raise NotImplementedError("the jump integrand g has no GPU kernel yet; pass ZeroFunction(d) as g")
-    else:
-        f = models
-    dim = f.kernel_dim() if hasattr(f, "kernel_dim") else None
+
+def _kernel_dim(net):
+    dim = net.kernel_dim() if hasattr(net, "kernel_dim") else None
     if dim is None:
         raise NotImplementedError("the GPU control-variate kernels implement Mlp(1+d, [64, 64, 64], d) with ReLU, "
                                   "no batch norm, d in {1, 2}")
-    return f, dim
+    return dim
+
+
+def kernel_models(models):
+    """[(net, dim, 'f' | 'g')] for the networks the kernels run: f, and g
+    unless it is a ZeroFunction.  Raises for architectures without a kernel."""
+    if isinstance(models, (list, tuple)):
+        f, g = models
+    else:
+        f, g = models, None
+    out = [(f, _kernel_dim(f), "f")]
+    if g is not None and not isinstance(g, ZeroFunction):
+        out.append((g, _kernel_dim(g), "g"))
+    return out
 
 
 def disc_rate(discounter):
@@ -175,26 +202,32 @@ def adam_hparams(opt):
     return float(lr if not torch.is_tensor(lr) else lr.item()), tuple(grp["betas"]), float(grp["eps"])
 
 
-def train_gpu(cv, data, rate, epochs, batch_size, lr, betas, eps, print_losses=False, early_stopping=None,
+def train_gpu(cvs, datas, rate, epochs, batch_size, lr, betas, eps, print_losses=False, early_stopping=None,
               generator=None):
-    """Minibatch training on device; returns the per-epoch mean losses."""
-    n = data.n
+    """Minibatch training of the networks ``cvs`` (one data set each, same
+    paths) on Var(Gamma); returns the per-epoch mean losses."""
+    n = datas[0].n
     nb = n // batch_size
     if nb < 1:
         raise ValueError("batch size %d larger than the %d training paths" % (batch_size, n))
+    dev = cvs[0].device
     loss_arr = []
     cost = 0.0
     for epoch in range(epochs):
         t0 = time.time()
-        perm = torch.randperm(n, device=cv.device, generator=generator)
-        losses = torch.zeros(nb, dtype=torch.float64, device=cv.device)
-        gamma = torch.empty(batch_size, dtype=torch.float32, device=cv.device)
+        perm = torch.randperm(n, device=dev, generator=generator)
+        losses = torch.zeros(nb, dtype=torch.float64, device=dev)
+        gamma = torch.empty(batch_size, dtype=torch.float32, device=dev)
         for b in range(nb):
             idx = perm[b * batch_size:(b + 1) * batch_size]
-            cv.forward(data, rate, idx, gamma)
+            cvs[0].forward(datas[0], rate, idx, gamma)
+            for cv, data in zip(cvs[1:], datas[1:]):
+                gamma += cv.forward(data, rate, idx)
             losses[b] = gamma.double().var()
-            cv.backward(data, rate, gamma, idx)
-            cv.adam(lr, betas, eps)
+            for cv, data in zip(cvs, datas):
+                cv.backward(data, rate, gamma, idx)
+            for cv in cvs:
+                cv.adam(lr, betas, eps)
         loss_arr.append(float(losses.mean()))
         if print_losses:
             print('{}: Train loss: {:.5f}     95% confidence interval: {:.5f}'.format(
@@ -217,31 +250,48 @@ def _gpu_state(f, dim, device):
     return st
 
 
+def _setup(models, dl, solver, device):
+    cvs, datas = [], []
+    for net, dim, role in kernel_models(models):
+        cvs.append(_gpu_state(net, dim, device))
+        if role == "f":
+            datas.append(CvData.from_dataset(dl.dataset, solver, device))
+        else:
+            datas.append(CvData.jumps_from_dataset(dl.dataset, solver, device))
+    return cvs, datas
+
+
+def gamma_gpu(cvs, datas, rate):
+    """Gamma of every path of the data sets (payoff + each network's term)."""
+    g = cvs[0].forward(datas[0], rate).clone()
+    for cv, data in zip(cvs[1:], datas[1:]):
+        g += cv.forward(data, rate)
+    return g
+
+
 def train_adapted_control_variates(models, opt, dl, solver, discounter, epochs=10, print_losses=True, tol=0,
                                    early_stopping=None):
-    """Train f on the dataset of ``dl`` (AdaptedPathData) with Adam; returns losses."""
+    """Train f (and g) on the dataset of ``dl`` (AdaptedPathData) with Adam;
+    returns the per-epoch losses (sde_mc/varred.py:134-199)."""
     if tol != 0:
         raise NotImplementedError("tol != 0 (dropping the last steps) is not implemented on the GPU")
-    f, dim = kernel_models(models)
     dev = N.require_cuda()
-    data = CvData.from_dataset(dl.dataset, solver, dev)
-    cv = _gpu_state(f, dim, dev)
+    cvs, datas = _setup(models, dl, solver, dev)
     lr, betas, eps = adam_hparams(opt)
-    losses = train_gpu(cv, data, disc_rate(discounter), epochs, int(dl.batch_size), lr, betas, eps, print_losses,
+    losses = train_gpu(cvs, datas, disc_rate(discounter), epochs, int(dl.batch_size), lr, betas, eps, print_losses,
                        early_stopping)
-    cv.write_back(opt)
+    for cv in cvs:
+        cv.write_back(opt)
     return losses
 
 
 def apply_adapted_control_variates(models, dl, solver, discounter, tol=0):
-    """(sum Gamma, sum Gamma^2) over the dataset of ``dl``."""
+    """(sum Gamma, sum Gamma^2) over the dataset of ``dl`` (sde_mc/varred.py:98-131)."""
     if tol != 0:
         raise NotImplementedError("tol != 0 is not implemented on the GPU")
-    f, dim = kernel_models(models)
     dev = N.require_cuda()
-    data = CvData.from_dataset(dl.dataset, solver, dev)
-    cv = _gpu_state(f, dim, dev)
-    g = cv.forward(data, disc_rate(discounter)).double()
+    cvs, datas = _setup(models, dl, solver, dev)
+    g = gamma_gpu(cvs, datas, disc_rate(discounter)).double()
     return g.sum(), (g * g).sum()
 
 
@@ -251,23 +301,20 @@ def train_diffusion_control_variate(model, opt, dl, solver, discounter, epochs, 
     start = time.time()
     if tol != 0:
         raise NotImplementedError("tol != 0 is not implemented on the GPU")
-    f, dim = kernel_models(model)
     dev = N.require_cuda()
-    data = CvData.from_dataset(dl.dataset, solver, dev)
-    cv = _gpu_state(f, dim, dev)
+    cvs, datas = _setup(model, dl, solver, dev)
     lr, betas, eps = adam_hparams(opt)
-    losses = train_gpu(cv, data, disc_rate(discounter), epochs, int(dl.batch_size), lr, betas, eps, print_losses,
+    losses = train_gpu(cvs, datas, disc_rate(discounter), epochs, int(dl.batch_size), lr, betas, eps, print_losses,
                        early_stopping)
-    cv.write_back(opt)
+    for cv in cvs:
+        cv.write_back(opt)
     return time.time() - start, losses
 
 
 def apply_diffusion_control_variate(model, dl, solver, discounter, tol=0):
     if tol != 0:
         raise NotImplementedError("tol != 0 is not implemented on the GPU")
-    f, dim = kernel_models(model)
     dev = N.require_cuda()
-    data = CvData.from_dataset(dl.dataset, solver, dev)
-    cv = _gpu_state(f, dim, dev)
-    g = cv.forward(data, disc_rate(discounter)).double()
+    cvs, datas = _setup(model, dl, solver, dev)
+    g = gamma_gpu(cvs, datas, disc_rate(discounter)).double()
     return g.sum(), (g * g).sum()

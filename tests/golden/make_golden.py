@@ -180,15 +180,55 @@ def f32(v):
     return float(np.float32(v))
 
 
+def cv_jump_fixture(sm, torch):
+    """The adapted control variate with both integrands (f on the Brownian
+    increments, g on the compensated jumps) through the reference's own
+    apply_adapted_control_variates and train_adapted_control_variates on one
+    64-path batch: the sums of Gamma, the first epoch's loss, the gradients
+    left on the parameters and the parameters after one Adam step."""
+    from torch.utils.data import DataLoader
+    torch.manual_seed(23)
+    corr = sm.get_corr_matrix([0.5])
+    m = sm.Merton(0.02, torch.tensor([0.2, 0.3]), 1.5, -0.05, 0.15, torch.tensor([1., 1.]), dim=2, corr_matrix=corr)
+    sol = sm.JumpEulerSolver(m, 1.0, 16)
+    csr = sm.ConstantShortRate(0.02)
+    ds = sm.simulate_adapted_data(64, sol, sm.Rainbow(1.0), csr, bs=64).dataset
+    dl = DataLoader(ds, batch_size=64, shuffle=False)
+    f = sm.Mlp(3, [64, 64, 64], 2, batch_norm=False, batch_norm_init=False)
+    g = sm.Mlp(3, [64, 64, 64], 2, batch_norm=False, batch_norm_init=False)
+    nets = {'f': f, 'g': g}
+    p0 = {k: [p.detach().clone() for p in v.parameters()] for k, v in nets.items()}
+    s1, s2 = sm.apply_adapted_control_variates([f, g], dl, sol, csr)
+    opt = torch.optim.Adam(list(f.parameters()) + list(g.parameters()), lr=1e-3)
+    losses = sm.train_adapted_control_variates([f, g], opt, dl, sol, csr, epochs=1, print_losses=False)
+    out = dict(time=ds.time_paths.numpy(), paths=ds.paths.numpy(), left=ds.left_paths.numpy(),
+               jumps=ds.jump_paths.numpy(), normals=ds.normals.numpy(), payoffs=ds.payoffs.numpy(),
+               sum=np.float64(float(s1)), sum_sq=np.float64(float(s2)), loss=np.float64(losses[0]),
+               lam_kappa=np.asarray(float(sol.sde.jump_rate() * sol.sde.jump_mean()), np.float32),
+               r=np.float32(0.02))
+    for k, v in nets.items():
+        for i, (a, p) in enumerate(zip(p0[k], v.parameters())):
+            out['p0%s_%d' % (k, i)] = a.numpy()
+            out['grad%s_%d' % (k, i)] = p.grad.detach().numpy()
+            out['p1%s_%d' % (k, i)] = p.detach().numpy()
+    np.savez_compressed(os.path.join(HERE, 'cv_mlp_jumps.npz'), **out)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--ref', default='/root/reference')
     ap.add_argument('--skip-stats', action='store_true')
+    ap.add_argument('--only', choices=['cv_jumps'], default=None,
+                    help='write only this fixture')
     args = ap.parse_args()
     sm = load_reference(args.ref)
     import torch
     torch.set_num_threads(min(8, os.cpu_count() or 1))
     t0 = time.time()
+    if args.only == 'cv_jumps':
+        cv_jump_fixture(sm, torch)
+        return
+    cv_jump_fixture(sm, torch)
 
     # ------------------------------------------------------------ KATs ----
     kat = {}

@@ -6,7 +6,9 @@ Tolerances: against the oracle's restatement of the kernels' precision policy
 (FP32 layers 1 and 4, BF16 64x64 layers with FP32 accumulation) the kernels
 agree to accumulation-order noise — outputs within 1e-3 of their largest
 magnitude, gradients within 3e-3 in relative norm.  Against the reference's
-FP32 network (fixture recorded from sde_mc) they agree to BF16 noise: 2%.
+FP32 network (fixtures recorded from sde_mc) they agree to BF16 noise: 2% on
+the Brownian-integrand fixture, 6% on the two-network fixture (where the BF16
+policy itself, restated on the CPU, is up to 4.3% off in relative norm).
 """
 import math
 
@@ -150,9 +152,77 @@ def test_training_reduces_variance_without_bias():
 def test_unsupported_models_raise():
     solver, payoff, disc = indep2d(8)
     dl = sm.simulate_adapted_data(64, solver, payoff, disc, bs=64, inference=True)
-    g = sm.Mlp(3, [64, 64, 64], 2, batch_norm=False, batch_norm_init=False)
+    g = sm.Mlp(3, [64, 64, 64], 2)  # batch norm: no kernel
     with pytest.raises(NotImplementedError):
         sm.apply_adapted_control_variates([_net(2), g], dl, solver, disc)
     with pytest.raises(NotImplementedError):
         sm.apply_adapted_control_variates([sm.Mlp(3, [32, 32], 2, batch_norm=False, batch_norm_init=False),
                                            sm.ZeroFunction(2)], dl, solver, disc)
+
+
+def _jump_fixture():
+    fx = load_npz("cv_mlp_jumps")
+    n, S, d = fx["normals"].shape
+    t = torch.from_numpy(fx["time"][..., 0])
+    t_full = torch.cat([t, torch.ones(n, 1)], 1)
+
+    def pad(a):
+        a = torch.from_numpy(a)
+        return torch.cat([a, a[:, -1:]], 1)
+    from oracle import oracle
+    mult = oracle.cv_jump_multipliers(fx["time"][..., 0], fx["jumps"], fx["lam_kappa"]).astype(np.float32)
+    data_f = V.CvData(t_full, pad(fx["paths"]), torch.from_numpy(fx["normals"]), torch.from_numpy(fx["payoffs"]), DEV)
+    data_g = V.CvData(t_full, pad(fx["left"]), torch.from_numpy(mult), torch.zeros(n), DEV)
+    pf = [fx["p0f_%d" % i] for i in range(8)]
+    pg = [fx["p0g_%d" % i] for i in range(8)]
+    return fx, data_f, data_g, pf, pg, mult
+
+
+def test_jump_integrand_matches_reference(oracle_mod):
+    """f and g together (two kernel passes, one Gamma): the sums, the loss and
+    both networks' gradients agree with the reference's own apply/train run
+    within BF16 noise, and with the oracle's precision-policy restatement to
+    accumulation noise."""
+    fx, data_f, data_g, pf, pg, mult = _jump_fixture()
+    r = float(fx["r"])
+    cf = V.GpuCv(_net(2, pf), 2, DEV)
+    cg = V.GpuCv(_net(2, pg), 2, DEV)
+    gamma = V.gamma_gpu([cf, cg], [data_f, data_g], r)
+    g64 = gamma.double()
+    assert float(g64.sum()) == pytest.approx(float(fx["sum"]), rel=2e-3)
+    assert float(g64.var()) == pytest.approx(float(fx["loss"]), rel=2e-2)
+    grad_f = cf.backward(data_f, r, gamma).cpu().numpy()
+    grad_g = cg.backward(data_g, r, gamma).cpu().numpy()
+    t = fx["time"][..., 0]
+    gm = gamma.cpu().numpy().astype(np.float64)
+    mixed_f = oracle_mod.cv_grads_mixed(pf, t, fx["paths"], fx["normals"], gm, r)
+    mixed_g = oracle_mod.cv_grads_mixed(pg, t, fx["left"], mult, gm, r)
+    for name, grad, mixed in (("f", grad_f, mixed_f), ("g", grad_g, mixed_g)):
+        off = 0
+        for i in range(8):
+            m = mixed[i].reshape(-1)
+            gi = grad[off:off + m.size]
+            off += m.size
+            assert np.linalg.norm(gi - m) <= 3e-3 * np.linalg.norm(m) + 1e-9, ("oracle", name, i)
+            ref = fx["grad%s_%d" % (name, i)].reshape(-1)
+            # the BF16 policy itself (oracle restatement) is up to 4.3% off the
+            # reference's FP32 gradients of f's first layers on this fixture
+            assert np.linalg.norm(gi - ref) <= 6e-2 * np.linalg.norm(ref) + 1e-9, ("reference", name, i)
+
+
+def test_training_with_jump_integrand():
+    """Merton 2D with common jumps: training f and g through the reference's
+    API on solver paths lowers the loss, and the estimate on fresh paths
+    agrees with the plain estimator within 3 standard errors."""
+    from tests.cases import merton2d_corr
+    solver, payoff, disc = merton2d_corr(32, seed=13)
+    f, g = _net(2, seed=6), _net(2, seed=7)
+    opt = torch.optim.Adam(list(f.parameters()) + list(g.parameters()), lr=1e-3)
+    dl = sm.simulate_adapted_data(1 << 15, solver, payoff, disc, bs=1024)
+    losses = sm.train_adapted_control_variates([f, g], opt, dl, solver, disc, epochs=4, print_losses=False)
+    assert losses[-1] < losses[0]
+    assert torch.equal(g.flat_params(DEV), g._sdemc_gpu.params)
+    st_cv = sm.mc_apply_cvs([f, g], solver, 1 << 15, payoff, disc, sim_bs=1 << 15, bs=1024)
+    st_plain = sm.mc_simple(1 << 16, solver, payoff, disc, bs=1 << 16, payoff_time='adapted')
+    assert st_cv.sample_std < st_plain.sample_std * math.sqrt(2)
+    assert abs(st_cv.sample_mean - st_plain.sample_mean) < 3 * math.hypot(st_cv.sample_std, st_plain.sample_std)

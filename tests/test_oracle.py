@@ -182,3 +182,23 @@ def test_chunk_reduce_matches_fp64_sum(oracle_mod):
     assert out[2] == 1000
     assert out[0] == pytest.approx(float(v.astype(np.float64).sum()), rel=1e-6)
     assert out[3] == pytest.approx(float(v.mean()), rel=1e-6)
+
+
+def test_cv_with_jump_integrand_restatement(oracle_mod):
+    """Both integrands of the reference's adapted control variate (f on the
+    Brownian increments, g on the marks minus lambda E[J] h): the oracle's
+    Gamma sums, loss and gradients of both networks equal what the reference's
+    own apply/train functions produced (fixture)."""
+    fx = load_npz("cv_mlp_jumps")
+    pf = [fx["p0f_%d" % i].astype(np.float64) for i in range(8)]
+    pg = [fx["p0g_%d" % i].astype(np.float64) for i in range(8)]
+    t = fx["time"][..., 0]
+    mult = oracle_mod.cv_jump_multipliers(t, fx["jumps"], fx["lam_kappa"])
+    loss, gamma, gf, gg = oracle_mod.cv2_loss_and_grads(pf, pg, t, fx["paths"], fx["left"], fx["normals"], mult,
+                                                        fx["payoffs"], float(fx["r"]))
+    assert loss == pytest.approx(float(fx["loss"]), rel=1e-5)
+    assert gamma.sum() == pytest.approx(float(fx["sum"]), rel=1e-5)
+    assert (gamma * gamma).sum() == pytest.approx(float(fx["sum_sq"]), rel=1e-5)
+    for i in range(8):
+        np.testing.assert_allclose(gf[i], fx["gradf_%d" % i], rtol=2e-3, atol=1e-6)
+        np.testing.assert_allclose(gg[i], fx["gradg_%d" % i], rtol=2e-3, atol=1e-6)
