@@ -173,6 +173,8 @@ class AdaptedPathData(Dataset):
         self.total_steps = total_steps
         self.full_paths = paths
         self.full_time = time_paths
+        self._full_left = left_paths
+        self._full_jumps = jump_paths
 
     def __len__(self):
         return len(self.payoffs)
@@ -180,6 +182,26 @@ class AdaptedPathData(Dataset):
     def __getitem__(self, idx):
         return (self.paths[idx], self.normals[idx], self.left_paths[idx],
                 self.time_paths[idx], self.jump_paths[idx]), self.payoffs[idx]
+
+    # ------------------------------------------------------- export/import --
+    def tensors(self):
+        """The full tensors (paths, payoffs, normals, left, time, jumps) as
+        materialised, last column included; on the device they were made on
+        (a DataLoader over this dataset hands them out without a copy)."""
+        return dict(paths=self.full_paths, payoffs=self.payoffs, normals=self.normals,
+                    left_paths=self._full_left, time_paths=self.full_time, jump_paths=self._full_jumps,
+                    total_steps=int(self.total_steps))
+
+    def save(self, path):
+        """Write the dataset to a ``.pt`` file (CPU tensors)."""
+        torch.save({k: (v.detach().cpu() if torch.is_tensor(v) else v) for k, v in self.tensors().items()}, path)
+
+    @classmethod
+    def load(cls, path, device="cpu"):
+        """Read a dataset written by :meth:`save` (onto ``device``)."""
+        d = torch.load(path, map_location=device, weights_only=True)
+        return cls(d["paths"], d["payoffs"], d["normals"], d["left_paths"], d["time_paths"], d["jump_paths"],
+                   d["total_steps"])
 
 
 def get_mlps(problem, num_layers, hidden_size, device):

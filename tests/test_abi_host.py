@@ -257,3 +257,27 @@ def test_torch_ops_registered_with_schemas():
     assert t.dtype == torch.uint8 and t.numel() == N.load().sdemc_inst_size()
     with pytest.raises(ValueError):
         torch_ops._inst(t[:-1])
+
+
+def test_adapted_path_data_round_trip(tmp_path):
+    """AdaptedPathData written to a .pt file and read back gives the same
+    tensors and the same DataLoader items (no GPU needed)."""
+    n, S, d = 8, 5, 2
+    g = torch.Generator().manual_seed(0)
+    paths = torch.rand((n, S + 1, d), generator=g)
+    normals = torch.randn((n, S, d), generator=g)
+    left = torch.rand((n, S + 1, d), generator=g)
+    time_p = torch.linspace(0, 1, S + 1).repeat(n, 1).unsqueeze(-1)
+    jumps = torch.zeros((n, S + 1, d))
+    payoffs = torch.rand(n, generator=g)
+    ds = sm.AdaptedPathData(paths, payoffs, normals, left, time_p, jumps, S)
+    f = tmp_path / "data.pt"
+    ds.save(str(f))
+    back = sm.AdaptedPathData.load(str(f))
+    for k, v in ds.tensors().items():
+        w = back.tensors()[k]
+        assert (torch.equal(v, w) if torch.is_tensor(v) else v == w), k
+    a, b = ds[3], back[3]
+    for x, y in zip(a[0], b[0]):
+        assert torch.equal(x, y)
+    assert torch.equal(a[1], b[1])
