@@ -339,6 +339,21 @@ int sdemc_adam_step(float* d_params, const float* d_grad, float* d_m, float* d_v
                     int nparam, int step, float lr, float beta1, float beta2,
                     float eps, void* stream);
 
+/* K5 on the 5th-generation tensor cores (tcgen05.mma, accumulators in tensor
+ * memory) for large batches: d_gamma[q] = payoff[index[q]] + sum_k
+ * e^{-r t_k} f(t_k, X_k) . d_mult[k] over the selected paths, where d_mult
+ * (N, S, d) holds each row's multipliers (the Brownian increments for the
+ * integrand f; marks minus compensator for the jump integrand g) and
+ * d_payoffs may be null (no payoff term).  d_scratch holds
+ * sdemc_cv_forward_tc_scratch_bytes(n, steps) bytes of per-range partial
+ * sums; a bounded wait that gives up sets SDEMC_ETIMEOUT in *d_status.    */
+size_t sdemc_cv_forward_tc_scratch_bytes(int64_t n, int steps);
+int sdemc_cv_forward_tc(int dim, const float* d_params, const float* d_time,
+                        const float* d_paths, const float* d_mult,
+                        const float* d_payoffs, const int64_t* d_index, int64_t n,
+                        int steps, float disc_rate, float* d_gamma, void* d_scratch,
+                        size_t scratch_bytes, int32_t* d_status, void* stream);
+
 /* ---- K9: pricing server (continuous batching) ---------------------------
  * A request is one run_mc (sde_mc/mc.py:418-440): a pilot of inst.num_paths
  * paths sizes the main run for a 95% half-width of rel_target * |price|

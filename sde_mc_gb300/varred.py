@@ -152,6 +152,26 @@ class GpuCv:
         N.check(rc, "sdemc_cv_forward")
         return gamma
 
+    def forward_tc(self, data, rate, idx=None, gamma=None):
+        """Gamma through the tcgen05 network kernel (large batches)."""
+        n = data.n if idx is None else int(idx.numel())
+        if gamma is None:
+            gamma = torch.empty(n, dtype=torch.float32, device=self.device)
+        lib = N.load()
+        need = lib.sdemc_cv_forward_tc_scratch_bytes(n, data.steps)
+        # own workspace: the shared scratch pool's header words belong to K1/K10
+        if getattr(self, "_tc_scratch", None) is None or self._tc_scratch.numel() < need:
+            self._tc_scratch = torch.empty(max(need, 1), dtype=torch.uint8, device=self.device)
+        scratch = self._tc_scratch
+        status = torch.zeros(1, dtype=torch.int32, device=self.device)
+        rc = lib.sdemc_cv_forward_tc(self.dim, N.ptr(self.params), N.ptr(data.time), N.ptr(data.paths),
+                                     N.ptr(data.normals), N.ptr(data.payoffs), N.ptr(idx), n, data.steps,
+                                     float(rate), N.ptr(gamma), N.ptr(scratch), scratch.numel(), N.ptr(status),
+                                     N.stream_handle(self.device))
+        N.check(rc, "sdemc_cv_forward_tc")
+        self._tc_status = status
+        return gamma
+
     def backward(self, data, rate, gamma, idx=None):
         n = data.n if idx is None else int(idx.numel())
         rc = N.load().sdemc_cv_backward(self.dim, N.ptr(self.params), N.ptr(data.time), N.ptr(data.paths),
