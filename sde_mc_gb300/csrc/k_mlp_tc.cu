@@ -20,9 +20,9 @@ cv_forward_tc_kernel(const float* __restrict__ prm, const float* __restrict__ ti
                      const float* __restrict__ mult, const int64_t* idx, int64_t n, int S, float rate, int nranges,
                      int range_len, float* __restrict__ partial, int32_t* status) {
   extern __shared__ unsigned char smem_raw[];
-  tc::TcSmem<D>& sm = *reinterpret_cast<tc::TcSmem<D>*>(
+  tc::TcSmem& sm = *reinterpret_cast<tc::TcSmem*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
-  tc::setup(sm, prm);
+  tc::setup<D>(sm, prm);
   uint32_t phase = 0;
   bool fail = false;
   const int64_t groups = (n + tc::kRows - 1) / tc::kRows;
@@ -94,7 +94,7 @@ static int launch_tc(const float* prm, const float* time, const float* paths, co
                      const float* payoffs, const int64_t* idx, int64_t n, int S, float rate, float* gamma,
                      float* partial, int32_t* status, int nranges, int range_len, cudaStream_t s) {
   auto kern = cv_forward_tc_kernel<D>;
-  const size_t smem = sizeof(tc::TcSmem<D>) + 1024;
+  const size_t smem = sizeof(tc::TcSmem) + 1024;
   int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                       "smem attribute");
   if (rc) return rc;

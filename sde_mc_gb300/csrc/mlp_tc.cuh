@@ -1,17 +1,25 @@
 // mlp_tc.cuh — the control-variate network on 5th-generation tensor cores.
 //
 // One CTA of 128 threads evaluates the network on 128 rows at a time, one row
-// per thread (a path's (t_k, X_k) at one step): layer 1 (1+d -> 64) in FP32 on
-// the CUDA cores, written as a BF16 A tile to shared memory in the canonical
-// no-swizzle K-major layout (8-row x 16-byte core matrices); the two 64x64
-// layers as tcgen05.mma kind::f16 (M = 128, N = 64, K = 16 x 4) issued by one
-// thread with FP32 accumulators in tensor memory (64 columns), completion
-// signalled on an mbarrier; tcgen05.ld brings each thread its row back for
-// bias + ReLU; layer 4 (64 -> d) in FP32.  The weights of the 64x64 layers
-// stay in shared memory (BF16, the same layout, B operands K-major).
+// per thread (a path's (t_k, X_k) at one step).  Three tcgen05.mma kind::f16
+// products (M = 128, issued by one thread, FP32 accumulators in 64 columns of
+// tensor memory, completion on an mbarrier) carry the first three layers:
+//
+//   layer 1 (1+d -> 64): K = 16.  FP32 accuracy from BF16 operands by
+//     splitting inputs and weights into high and low BF16 parts:
+//     x w ~ xh wh + xl wh + xh wl (the dropped xl wl is ~2^-16 relative), the
+//     bias as bh + bl against two ones columns;
+//   layers 2, 3 (64 -> 64): K = 80 = 64 activations + the bias (high, low)
+//     against two ones columns + 14 zero columns.
+//
+// Operands sit in shared memory in the canonical no-swizzle K-major layout
+// (8-row x 16-byte core matrices; K-adjacent core matrices 128 B apart, row
+// groups K/8 x 128 B apart).  After each product every thread reads its own
+// row back with tcgen05.ld, applies ReLU and writes the BF16 row of the next
+// A tile; layer 4 (64 -> d) stays in FP32 on the CUDA cores.
 //
 // Every wait on the mbarrier is bounded; a CTA that gives up records
-// SDEMC_ETIMEOUT and stops issuing work, and always frees its tensor memory.
+// SDEMC_ETIMEOUT, stops issuing work and always frees its tensor memory.
 #pragma once
 #include "sdemc_device.cuh"
 #include <cuda_bf16.h>
@@ -20,14 +28,12 @@ namespace sdemc {
 namespace tc {
 
 constexpr int kRows = 128;        // M: rows per tile = threads per CTA
-constexpr int kH = 64;            // hidden width (N and K of the 64x64 layers)
+constexpr int kH = 64;            // hidden width (N of every product)
+constexpr int kK1 = 16;           // K of layer 1 (split inputs, bias)
+constexpr int kKH = 80;           // K of layers 2, 3 (64 + bias + padding)
 constexpr int kTmemCols = 64;     // FP32 accumulator columns
-constexpr uint32_t kCoreRowBytes = 16;                   // one core-matrix row: 8 bf16
-constexpr uint32_t kLbo = 128;                           // K-adjacent core matrices (8 rows x 16 B)
-constexpr uint32_t kSbo = (kH / 8) * 128;                // M/N-adjacent core-matrix rows: 1024 B
-constexpr uint32_t kTileBytesA = kRows * kH * 2;         // 16 KB
-constexpr uint32_t kTileBytesB = kH * kH * 2;            // 8 KB
-constexpr int kMaxSpins = 1 << 22;                       // bound of one mbarrier wait
+constexpr uint32_t kLbo = 128;    // K-adjacent core matrices
+constexpr int kMaxSpins = 1 << 22;  // bound of one mbarrier wait
 
 // instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16
 // (bits 7-9 = 1, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 in bits
@@ -35,17 +41,17 @@ constexpr int kMaxSpins = 1 << 22;                       // bound of one mbarrie
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kH >> 3) << 17) |
                             ((uint32_t)(kRows >> 4) << 24);
 
-// Byte offset of element (r, k) of a K-major bf16 matrix with 64 columns in
+// Byte offset of element (r, k) of a K-major bf16 matrix with K columns in
 // the canonical no-swizzle layout.
-SDEMC_HDI uint32_t core_offset(int r, int k) {
-  return (uint32_t)(r >> 3) * kSbo + (uint32_t)(k >> 3) * kLbo + (uint32_t)(r & 7) * kCoreRowBytes +
+SDEMC_HDI uint32_t core_offset(int r, int k, int K) {
+  return (uint32_t)(r >> 3) * (uint32_t)(K / 8) * 128u + (uint32_t)(k >> 3) * kLbo + (uint32_t)(r & 7) * 16u +
          (uint32_t)(k & 7) * 2u;
 }
 
 // Shared-memory matrix descriptor: start >> 4 (bits 0-13), LBO >> 4 (16-29),
 // SBO >> 4 (32-45), version 1 (bits 46-47), no swizzle (bits 61-63 = 0).
-SDEMC_DI uint64_t smem_desc(uint32_t saddr) {
-  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(kLbo >> 4) << 16) | ((uint64_t)(kSbo >> 4) << 32) |
+SDEMC_DI uint64_t smem_desc(uint32_t saddr, uint32_t sbo) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(kLbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
          (1ull << 46);
 }
 
@@ -97,86 +103,6 @@ SDEMC_DI void mma_commit(uint32_t mbar_saddr) {
                : "memory");
 }
 
-SDEMC_DI void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
-
-SDEMC_DI uint32_t pack2(float lo, float hi) {
-  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-  return *reinterpret_cast<const uint32_t*>(&v);
-}
-
-// Shared memory of one CTA (placed at a 1024-byte aligned address).
-template <int D>
-struct TcSmem {
-  unsigned char A[kTileBytesA];   // activations, 128 x 64 bf16
-  unsigned char B2[kTileBytesB];  // W2 (out x in), bf16, K-major
-  unsigned char B3[kTileBytesB];  // W3
-  float w1[kH * (D + 1)], b1[kH], b2[kH], b3[kH], w4[D * kH], b4[D];
-  unsigned long long mbar;
-  uint32_t tmem;
-};
-
-// Parameter vector offsets (torch order: W1, b1, W2, b2, W3, b3, W4, b4).
-template <int D> struct TcLayout {
-  static constexpr int IN = D + 1;
-  static constexpr int W1 = 0, B1 = W1 + kH * IN, W2 = B1 + kH, B2 = W2 + kH * kH, W3 = B2 + kH,
-                       B3 = W3 + kH * kH, W4 = B3 + kH, B4 = W4 + D * kH, N = B4 + D;
-};
-
-// CTA-wide setup: weights into shared memory, mbarrier, tensor memory.
-template <int D>
-SDEMC_DI void setup(TcSmem<D>& sm, const float* prm) {
-  using L = TcLayout<D>;
-  const int t = threadIdx.x;
-  for (int e = t; e < kH * kH; e += blockDim.x) {
-    const int n = e / kH, k = e % kH;
-    *reinterpret_cast<__nv_bfloat16*>(sm.B2 + core_offset(n, k)) = __float2bfloat16_rn(prm[L::W2 + e]);
-    *reinterpret_cast<__nv_bfloat16*>(sm.B3 + core_offset(n, k)) = __float2bfloat16_rn(prm[L::W3 + e]);
-  }
-  for (int e = t; e < kH * L::IN; e += blockDim.x) sm.w1[e] = prm[L::W1 + e];
-  for (int e = t; e < kH; e += blockDim.x) {
-    sm.b1[e] = prm[L::B1 + e];
-    sm.b2[e] = prm[L::B2 + e];
-    sm.b3[e] = prm[L::B3 + e];
-  }
-  for (int e = t; e < D * kH; e += blockDim.x) sm.w4[e] = prm[L::W4 + e];
-  if (t < D) sm.b4[t] = prm[L::B4 + t];
-  if (t == 0) {
-    mbar_init(saddr_of(&sm.mbar));
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  fence_async_smem();  // B tiles: generic-proxy stores, read by the tensor cores
-  if (t < 32) tmem_alloc(saddr_of(&sm.tmem));
-  fence_before_sync();
-  __syncthreads();
-  fence_after_sync();
-}
-
-template <int D>
-SDEMC_DI void teardown(TcSmem<D>& sm) {
-  fence_before_sync();
-  __syncthreads();
-  fence_after_sync();
-  if (threadIdx.x < 32) tmem_dealloc(sm.tmem);
-}
-
-// One 64x64 layer for the CTA's 128 rows: A (already in smem, fenced and
-// synchronised) x W -> TMEM; returns false if the wait gave up.
-template <int D>
-SDEMC_DI bool layer_mma(TcSmem<D>& sm, const unsigned char* B, uint32_t& phase) {
-  if (threadIdx.x == 0) {
-    fence_after_sync();
-    const uint32_t a0 = saddr_of(sm.A), b0 = saddr_of(B);
-#pragma unroll
-    for (int kk = 0; kk < kH / 16; ++kk)
-      mma_f16(sm.tmem, smem_desc(a0 + kk * 2 * kLbo), smem_desc(b0 + kk * 2 * kLbo), kk > 0 ? 1u : 0u);
-    mma_commit(saddr_of(&sm.mbar));
-  }
-  const bool ok = mbar_wait(saddr_of(&sm.mbar), phase);
-  phase ^= 1u;
-  fence_after_sync();
-  return ok;
-}
-
 // 16 consecutive FP32 columns of this thread's TMEM lane.
 SDEMC_DI void tmem_ld16(uint32_t taddr, float* v) {
   uint32_t r[16];
@@ -190,13 +116,128 @@ SDEMC_DI void tmem_ld16(uint32_t taddr, float* v) {
 #pragma unroll
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
+SDEMC_DI void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 SDEMC_DI uint32_t lane_base() { return (uint32_t)((threadIdx.x >> 5) * 32) << 16; }
 
-// Accumulator row + bias, ReLU, as the next layer's BF16 A row; 16 columns
-// at a time so that few values are live.
+SDEMC_DI uint32_t pack2(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+SDEMC_DI uint32_t pack2b(__nv_bfloat16 lo, __nv_bfloat16 hi) {
+  return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+}
+SDEMC_HDI void split(float v, __nv_bfloat16& h, __nv_bfloat16& l) {
+  h = __float2bfloat16_rn(v);
+  l = __float2bfloat16_rn(v - __bfloat162float(h));
+}
+
+// Shared memory of one CTA (placed at a 1024-byte aligned address).
+struct TcSmem {
+  unsigned char A[kRows * kKH * 2];   // activations of layers 2, 3 (+ ones columns)
+  unsigned char A1[kRows * kK1 * 2];  // split inputs of layer 1
+  unsigned char B1[kH * kK1 * 2];     // split W1 and b1
+  unsigned char B2[kH * kKH * 2];     // W2 | b2 (high, low), K-major
+  unsigned char B3[kH * kKH * 2];
+  float2 w4[kH];                      // W4 columns (d <= 2)
+  float b4[2];
+  unsigned long long mbar;
+  uint32_t tmem;
+};
+
+// Parameter vector offsets (torch order: W1, b1, W2, b2, W3, b3, W4, b4).
+template <int D> struct TcLayout {
+  static constexpr int IN = D + 1;
+  static constexpr int W1 = 0, B1 = W1 + kH * IN, W2 = B1 + kH, B2 = W2 + kH * kH, W3 = B2 + kH,
+                       B3 = W3 + kH * kH, W4 = B3 + kH, B4 = W4 + D * kH, N = B4 + D;
+};
+
+SDEMC_DI void put_bf16(unsigned char* M, int r, int k, int K, __nv_bfloat16 v) {
+  *reinterpret_cast<__nv_bfloat16*>(M + core_offset(r, k, K)) = v;
+}
+
+// CTA-wide setup: operands into shared memory, mbarrier, tensor memory.
 template <int D>
-SDEMC_DI void relu_to_A(TcSmem<D>& sm, const float* bias) {
+SDEMC_DI void setup(TcSmem& sm, const float* prm) {
+  using L = TcLayout<D>;
+  const int t = threadIdx.x;
+  const __nv_bfloat16 one = __float2bfloat16_rn(1.f), zero = __float2bfloat16_rn(0.f);
+  for (int e = t; e < kH * kKH; e += blockDim.x) {
+    const int n = e / kKH, k = e % kKH;
+    __nv_bfloat16 v2 = zero, v3 = zero;
+    if (k < kH) {
+      v2 = __float2bfloat16_rn(prm[L::W2 + n * kH + k]);
+      v3 = __float2bfloat16_rn(prm[L::W3 + n * kH + k]);
+    } else if (k < kH + 2) {
+      __nv_bfloat16 h, l;
+      split(prm[L::B2 + n], h, l);
+      v2 = k == kH ? h : l;
+      split(prm[L::B3 + n], h, l);
+      v3 = k == kH ? h : l;
+    }
+    put_bf16(sm.B2, n, k, kKH, v2);
+    put_bf16(sm.B3, n, k, kKH, v3);
+  }
+  // layer 1: columns 3i, 3i+1, 3i+2 of input i = (xh, xl, xh) against
+  // (wh, wh, wl); columns 3(D+1), +1 = ones against (bh, bl)
+  for (int e = t; e < kH * kK1; e += blockDim.x) {
+    const int n = e / kK1, k = e % kK1;
+    __nv_bfloat16 v = zero;
+    if (k < 3 * (D + 1)) {
+      __nv_bfloat16 h, l;
+      split(prm[L::W1 + n * L::IN + k / 3], h, l);
+      v = (k % 3 == 2) ? l : h;
+    } else if (k < 3 * (D + 1) + 2) {
+      __nv_bfloat16 h, l;
+      split(prm[L::B1 + n], h, l);
+      v = k == 3 * (D + 1) ? h : l;
+    }
+    put_bf16(sm.B1, n, k, kK1, v);
+  }
+  // the A tile's bias and padding columns never change: ones, then zeros
+  for (int e = t; e < kRows * (kKH - kH); e += blockDim.x) {
+    const int r = e / (kKH - kH), k = kH + e % (kKH - kH);
+    put_bf16(sm.A, r, k, kKH, k < kH + 2 ? one : zero);
+  }
+  for (int j = t; j < kH; j += blockDim.x)
+    sm.w4[j] = make_float2(prm[L::W4 + j], D > 1 ? prm[L::W4 + kH + j] : 0.f);
+  if (t < D) sm.b4[t] = prm[L::B4 + t];
+  if (t == 0) {
+    mbar_init(saddr_of(&sm.mbar));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  fence_async_smem();  // generic-proxy stores, read by the tensor cores
+  if (t < 32) tmem_alloc(saddr_of(&sm.tmem));
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+}
+
+SDEMC_DI void teardown(TcSmem& sm) {
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  if (threadIdx.x < 32) tmem_dealloc(sm.tmem);
+}
+
+// One product for the CTA's 128 rows: A (already in smem, fenced and
+// synchronised) x B -> TMEM over K columns; false if the wait gave up.
+SDEMC_DI bool product(TcSmem& sm, const unsigned char* A, const unsigned char* B, int K, uint32_t& phase) {
+  if (threadIdx.x == 0) {
+    fence_after_sync();
+    const uint32_t a0 = saddr_of(A), b0 = saddr_of(B), sbo = (uint32_t)(K / 8) * 128u;
+    for (int kk = 0; kk < K / 16; ++kk)
+      mma_f16(sm.tmem, smem_desc(a0 + kk * 2 * kLbo, sbo), smem_desc(b0 + kk * 2 * kLbo, sbo), kk > 0 ? 1u : 0u);
+    mma_commit(saddr_of(&sm.mbar));
+  }
+  const bool ok = mbar_wait(saddr_of(&sm.mbar), phase);
+  phase ^= 1u;
+  fence_after_sync();
+  return ok;
+}
+
+// Accumulator row (bias included), ReLU, as the next A row (BF16).
+SDEMC_DI void relu_to_A(TcSmem& sm) {
   const uint32_t base = sm.tmem + lane_base();
 #pragma unroll
   for (int c = 0; c < kH / 16; ++c) {
@@ -204,26 +245,22 @@ SDEMC_DI void relu_to_A(TcSmem<D>& sm, const float* bias) {
     tmem_ld16(base + 16 * c, v);
     tmem_ld_wait();
 #pragma unroll
-    for (int j = 0; j < 16; ++j) v[j] = fmaxf(__fadd_rn(v[j], bias[16 * c + j]), 0.f);
-#pragma unroll
     for (int h = 0; h < 2; ++h) {
       uint4 q;
-      q.x = pack2(v[8 * h + 0], v[8 * h + 1]);
-      q.y = pack2(v[8 * h + 2], v[8 * h + 3]);
-      q.z = pack2(v[8 * h + 4], v[8 * h + 5]);
-      q.w = pack2(v[8 * h + 6], v[8 * h + 7]);
-      *reinterpret_cast<uint4*>(sm.A + core_offset(threadIdx.x, 16 * c + 8 * h)) = q;
+      q.x = pack2(fmaxf(v[8 * h + 0], 0.f), fmaxf(v[8 * h + 1], 0.f));
+      q.y = pack2(fmaxf(v[8 * h + 2], 0.f), fmaxf(v[8 * h + 3], 0.f));
+      q.z = pack2(fmaxf(v[8 * h + 4], 0.f), fmaxf(v[8 * h + 5], 0.f));
+      q.w = pack2(fmaxf(v[8 * h + 6], 0.f), fmaxf(v[8 * h + 7], 0.f));
+      *reinterpret_cast<uint4*>(sm.A + core_offset(threadIdx.x, 16 * c + 8 * h, kKH)) = q;
     }
   }
 }
 
-// Accumulator row + bias, ReLU, then layer 4 (64 -> d) in FP32.
+// Accumulator row (bias included), ReLU, then layer 4 (64 -> d) in FP32.
 template <int D>
-SDEMC_DI void relu_layer4(TcSmem<D>& sm, float* out) {
+SDEMC_DI void relu_layer4(TcSmem& sm, float* out) {
   const uint32_t base = sm.tmem + lane_base();
-  float o[D];
-#pragma unroll
-  for (int i = 0; i < D; ++i) o[i] = 0.f;
+  float o0 = 0.f, o1 = 0.f;
 #pragma unroll
   for (int c = 0; c < kH / 16; ++c) {
     float v[16];
@@ -231,36 +268,41 @@ SDEMC_DI void relu_layer4(TcSmem<D>& sm, float* out) {
     tmem_ld_wait();
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
-      const float h = fmaxf(__fadd_rn(v[j], sm.b3[16 * c + j]), 0.f);
-#pragma unroll
-      for (int i = 0; i < D; ++i) o[i] = __fmaf_rn(sm.w4[i * kH + 16 * c + j], h, o[i]);
+      const float h = fmaxf(v[j], 0.f);
+      const float2 w = sm.w4[16 * c + j];
+      o0 = __fmaf_rn(w.x, h, o0);
+      if (D > 1) o1 = __fmaf_rn(w.y, h, o1);
     }
   }
-#pragma unroll
-  for (int i = 0; i < D; ++i) out[i] = __fadd_rn(o[i], sm.b4[i]);
+  out[0] = __fadd_rn(o0, sm.b4[0]);
+  if (D > 1) out[1] = __fadd_rn(o1, sm.b4[1]);
 }
 
-// Layer 1 (FP32) of this thread's row, written as the BF16 A row.
+// Layer 1's A row: (th, tl, th, x0h, x0l, x0h, ..., 1, 1, 0 ...).
 template <int D>
-SDEMC_DI void layer1_to_A(TcSmem<D>& sm, float t, const float* x) {
-  using L = TcLayout<D>;
+SDEMC_DI void inputs_to_A1(TcSmem& sm, float t, const float* x) {
+  __nv_bfloat16 a[kK1];
+  const __nv_bfloat16 one = __float2bfloat16_rn(1.f), zero = __float2bfloat16_rn(0.f);
 #pragma unroll
-  for (int c = 0; c < kH / 8; ++c) {
-    float h[8];
+  for (int i = 0; i <= D; ++i) {
+    __nv_bfloat16 h, l;
+    split(i == 0 ? t : x[i - 1], h, l);
+    a[3 * i] = h;
+    a[3 * i + 1] = l;
+    a[3 * i + 2] = h;
+  }
+  a[3 * (D + 1)] = one;
+  a[3 * (D + 1) + 1] = one;
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      const int j = 8 * c + u;
-      float z = __fmaf_rn(sm.w1[j * L::IN], t, sm.b1[j]);
+  for (int k = 3 * (D + 1) + 2; k < kK1; ++k) a[k] = zero;
 #pragma unroll
-      for (int i = 0; i < D; ++i) z = __fmaf_rn(sm.w1[j * L::IN + 1 + i], x[i], z);
-      h[u] = fmaxf(z, 0.f);
-    }
+  for (int c = 0; c < kK1 / 8; ++c) {
     uint4 q;
-    q.x = pack2(h[0], h[1]);
-    q.y = pack2(h[2], h[3]);
-    q.z = pack2(h[4], h[5]);
-    q.w = pack2(h[6], h[7]);
-    *reinterpret_cast<uint4*>(sm.A + core_offset(threadIdx.x, 8 * c)) = q;
+    q.x = pack2b(a[8 * c + 0], a[8 * c + 1]);
+    q.y = pack2b(a[8 * c + 2], a[8 * c + 3]);
+    q.z = pack2b(a[8 * c + 4], a[8 * c + 5]);
+    q.w = pack2b(a[8 * c + 6], a[8 * c + 7]);
+    *reinterpret_cast<uint4*>(sm.A1 + core_offset(threadIdx.x, 8 * c, kK1)) = q;
   }
 }
 
@@ -270,19 +312,24 @@ SDEMC_DI void layer1_to_A(TcSmem<D>& sm, float t, const float* x) {
 // barriers agree on it (__syncthreads_or), so once any thread's wait gave up
 // every thread returns false from then on without touching the tensor cores.
 template <int D>
-SDEMC_DI bool forward_rows(TcSmem<D>& sm, float t, const float* x, float* out, uint32_t& phase, bool& fail) {
-  layer1_to_A(sm, t, x);
+SDEMC_DI bool forward_rows(TcSmem& sm, float t, const float* x, float* out, uint32_t& phase, bool& fail) {
+  inputs_to_A1<D>(sm, t, x);
   fence_async_smem();
   fence_before_sync();
   if (__syncthreads_or(fail)) { fail = true; return false; }
-  bool ok = layer_mma(sm, sm.B2, phase);
-  if (ok) relu_to_A(sm, sm.b2);
+  bool ok = product(sm, sm.A1, sm.B1, kK1, phase);
+  if (ok) relu_to_A(sm);
   fence_async_smem();
   fence_before_sync();
   if (__syncthreads_or(!ok)) { fail = true; return false; }
-  ok = layer_mma(sm, sm.B3, phase);
+  ok = product(sm, sm.A, sm.B2, kKH, phase);
+  if (ok) relu_to_A(sm);
+  fence_async_smem();
+  fence_before_sync();
+  if (__syncthreads_or(!ok)) { fail = true; return false; }
+  ok = product(sm, sm.A, sm.B3, kKH, phase);
   if (!ok) { fail = true; return false; }
-  relu_layer4(sm, out);
+  relu_layer4<D>(sm, out);
   return true;
 }
 

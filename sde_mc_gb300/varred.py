@@ -281,11 +281,21 @@ def _setup(models, dl, solver, device):
     return cvs, datas
 
 
+TC_MIN_PATHS = 1 << 14  # below this the warp-level mma.sync kernel fills the GPU better
+
+
 def gamma_gpu(cvs, datas, rate):
-    """Gamma of every path of the data sets (payoff + each network's term)."""
-    g = cvs[0].forward(datas[0], rate).clone()
+    """Gamma of every path of the data sets (payoff + each network's term):
+    the tcgen05 network kernel for large sets, the mma.sync one for small."""
+    def fwd(cv, data):
+        if data.n >= TC_MIN_PATHS:
+            out = cv.forward_tc(data, rate)
+            N.status_error(int(cv._tc_status.item()), "control-variate network (tensor cores)")
+            return out
+        return cv.forward(data, rate)
+    g = fwd(cvs[0], datas[0]).clone()
     for cv, data in zip(cvs[1:], datas[1:]):
-        g += cv.forward(data, rate)
+        g += fwd(cv, data)
     return g
 
 
