@@ -477,8 +477,9 @@ def bench_cv_learned(dev, epochs=10):
             "regression_cv_same_model": {"vrf": reg[2].vrf, "mean": reg[2].mean, "se": reg[2].se,
                                          "plain_mean": reg[1].mean, "plain_se": reg[1].se,
                                          "main_paths_cv": reg[2].main_paths, "main_paths_plain": reg[1].main_paths},
-            "note": "the plain estimate uses the same 2^22 fresh paths as the control-variate estimate; eval time "
-                    "includes materialising the paths (K4)"}
+            "eval_kernel": "K7 price_cv_kernel: paths + payoff + network on tcgen05 in one pass",
+            "note": "the plain estimate uses the same 2^22 fresh paths as the control-variate estimate; eval "
+                    "simulates the paths inside the same kernel (nothing materialised)"}
 
 
 def shard(reqs, rank, world):

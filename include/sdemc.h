@@ -348,6 +348,17 @@ int sdemc_adam_step(float* d_params, const float* d_grad, float* d_m, float* d_v
  * sdemc_cv_forward_tc_scratch_bytes(n, steps) bytes of per-range partial
  * sums; a bounded wait that gives up sets SDEMC_ETIMEOUT in *d_status.    */
 size_t sdemc_cv_forward_tc_scratch_bytes(int64_t n, int steps);
+
+/* K7: paths, payoff and the learned control variate (integrand f, g = 0) in
+ * one pass, no materialised paths (apply_adapted_control_variates,
+ * sde_mc/varred.py:98-131).  The network runs on the tensor cores at every
+ * step of 128 paths per CTA.  d_out receives 8 doubles: sum Gamma,
+ * sum Gamma^2, n, sum payoff, sum payoff^2, mean Gamma, var Gamma, status;
+ * d_gamma (nullable) the per-path Gamma.  Diagonal noise, d in {1, 2}.    */
+size_t sdemc_price_cv_scratch_bytes(const sdemc_inst* h_inst);
+int sdemc_price_cv(const sdemc_inst* h_inst, const float* d_params, float disc_rate,
+                   void* d_scratch, size_t scratch_bytes, double* d_out,
+                   float* d_gamma, void* stream);
 int sdemc_cv_forward_tc(int dim, const float* d_params, const float* d_time,
                         const float* d_paths, const float* d_mult,
                         const float* d_payoffs, const int64_t* d_index, int64_t n,

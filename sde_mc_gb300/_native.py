@@ -88,6 +88,8 @@ _PROTOS = {
     "sdemc_cv_forward_tc_scratch_bytes": (ctypes.c_size_t, [ctypes.c_int64, _I]),
     "sdemc_cv_forward_tc": (_I, [_I, _P, _P, _P, _P, _P, _P, ctypes.c_int64, _I, ctypes.c_float, _P, _P,
                                  ctypes.c_size_t, _P, _P]),
+    "sdemc_price_cv_scratch_bytes": (ctypes.c_size_t, [_P]),
+    "sdemc_price_cv": (_I, [_P, _P, ctypes.c_float, _P, ctypes.c_size_t, _P, _P, _P]),
     "sdemc_price_noalloc_scratch_bytes": (ctypes.c_size_t, []),
     "sdemc_price_noalloc": (_I, [_P, _P, _P, _P, _P]),
     "sdemc_replay": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),

@@ -555,6 +555,9 @@ struct StoreSink {
 // sde_mc/mc.py:84-86, 92).
 constexpr int kModeExact = 1;
 constexpr int kModeNominal = 2;
+// All warps of the CTA step together (the loop runs while any lane of the CTA
+// is active): for sinks that evaluate something CTA-wide at every step.
+constexpr int kModeCtaSync = 4;
 
 // One path per lane; the warp steps in lock-step so that step k of every lane
 // draws from block k of its own stream (warp-uniform control, no divergence
@@ -596,7 +599,7 @@ SDEMC_DI int simulate(const sdemc_inst& I, Draws& dr, Sink& sk, float* x, int ma
 #pragma unroll
     for (int i = 0; i < D; ++i) xcap[i] = x[i];
   }
-  while (__any_sync(kFull, act)) {
+  while ((MODE & kModeCtaSync) ? __syncthreads_or(act) : __any_sync(kFull, act)) {
     if (k >= max_iters) { overflow = true; break; }
     // h = min(h, max(T - t, 0)); dt = min(h, next_jump - t)
     h = fminf(h, fmaxf(__fsub_rn(T, t), 0.f));

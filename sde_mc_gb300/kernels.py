@@ -48,6 +48,25 @@ def mlmc_level(inst, fine, coarse, h_fine, h_coarse, cfg=None, ys=None, device=N
     return out
 
 
+def price_cv(inst, params, disc_rate, gamma=None, device=None, out=None):
+    """K7: paths + payoff + learned control variate (f on the tensor cores) in
+    one launch.  Returns float64 CUDA tensor (sum G, sum G^2, n, sum P,
+    sum P^2, mean G, var G, status); ``gamma`` (nullable, float32 (n,))
+    receives each path's Gamma."""
+    dev = _dev(device)
+    lib = N.load()
+    need = lib.sdemc_price_cv_scratch_bytes(ctypes.byref(inst))
+    scratch = N.SCRATCH.get(need, dev)
+    if out is None:
+        out = torch.empty(8, dtype=torch.float64, device=dev)
+    if gamma is not None:
+        assert gamma.is_cuda and gamma.dtype == torch.float32 and gamma.numel() >= inst.num_paths
+    rc = lib.sdemc_price_cv(ctypes.byref(inst), N.ptr(params), float(disc_rate), N.ptr(scratch), scratch.numel(),
+                            N.ptr(out), N.ptr(gamma), N.stream_handle(dev))
+    N.check(rc, "sdemc_price_cv")
+    return out
+
+
 def zdim(dim, noise):
     return dim if noise == N.NOISE_DIAG else (dim + 1 if noise == N.NOISE_INDEP_SHARED else 2 * dim)
 

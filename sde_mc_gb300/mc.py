@@ -215,9 +215,15 @@ def mc_apply_cvs(models, solver, trials, payoff, discounter, sim_bs=1e5, bs=1000
     """Plain estimate of Gamma = payoff + control variate over fresh paths
     (sde_mc/mc.py:195-242)."""
     from .helpers import mc_estimates
-    from .varred import apply_adapted_control_variates, apply_diffusion_control_variate
+    from .varred import (apply_adapted_control_variates, apply_diffusion_control_variate, fused_cv_stats,
+                         fused_supported)
     start = time.time()
     trials = int(trials)
+    if solver.has_jumps and fused_supported(models, solver, discounter, tol):
+        # K7: the same fresh paths, simulated and evaluated in one pass
+        r = fused_cv_stats(models, solver, payoff, discounter, trials).cpu().tolist()
+        N.status_error(r[7], "mc_apply_cvs")
+        return MCStatistics(r[5], math.sqrt(max(r[6], 0.0)) / math.sqrt(trials), time.time() - start, trials)
     s = s2 = 0.0
     left = trials
     while left > 0:

@@ -27,12 +27,19 @@ def _level(solver, payoff, discounter, n, fine, coarse):
 
 
 def level_estimates(trials, levels, solver, payoff, discounter):
-    """Launch every level, then read back (mean, var) per level in FP64."""
-    outs = [_level0(solver, payoff, discounter, trials[0], levels[0])]
+    """Launch every level, then read back (mean, var) per level in FP64.  A
+    level allotted no paths (Giles' allocation gives N_l = 0 when the pilot
+    saw V_l = 0, e.g. fine and coarse grids made only of jump times) is not
+    launched and contributes (0, 0)."""
+    outs = [_level0(solver, payoff, discounter, trials[0], levels[0]) if trials[0] > 0 else None]
     for i in range(1, len(levels)):
-        outs.append(_level(solver, payoff, discounter, trials[i], levels[i], levels[i - 1]))
+        outs.append(_level(solver, payoff, discounter, trials[i], levels[i], levels[i - 1]) if trials[i] > 0
+                    else None)
     est = []
     for i, o in enumerate(outs):
+        if o is None:
+            est.append((0.0, 0.0))
+            continue
         r = o.cpu().tolist()
         if i == 0:
             N.status_error(r[5], "mc_multilevel level 0")
@@ -49,7 +56,7 @@ def mc_multilevel(trials, levels, solver, payoff, discounter, bs=None):
     trials = [int(t) for t in trials]
     est = level_estimates(trials, levels, solver, payoff, discounter)
     mean = sum(m for m, _ in est)
-    sd = math.sqrt(sum(v / n for (_, v), n in zip(est, trials)))
+    sd = math.sqrt(sum(v / n for (_, v), n in zip(est, trials) if n > 0))
     return MCStatistics(mean, sd, time.time() - start, trials[-1])
 
 

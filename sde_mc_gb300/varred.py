@@ -348,3 +348,34 @@ def apply_diffusion_control_variate(model, dl, solver, discounter, tol=0):
     cvs, datas = _setup(model, dl, solver, dev)
     g = gamma_gpu(cvs, datas, disc_rate(discounter)).double()
     return g.sum(), (g * g).sum()
+
+
+def fused_supported(models, solver, discounter, tol=0):
+    """True when K7 (paths + payoff + f in one pass) can price the control
+    variate: f a supported Mlp, g = ZeroFunction, diagonal noise, d in {1, 2},
+    a constant short rate and no dropped steps."""
+    if tol != 0 or getattr(discounter, "r", None) is None:
+        return False
+    try:
+        nets = kernel_models(models)
+    except NotImplementedError:
+        return False
+    if len(nets) != 1:
+        return False
+    from .lowering import lower
+    try:
+        inst = lower(solver, None, discounter, num_paths=1)
+    except NotImplementedError:
+        return False
+    return inst.noise == N.NOISE_DIAG and inst.dim in (1, 2) and inst.dim == nets[0][1]
+
+
+def fused_cv_stats(models, solver, payoff, discounter, trials, gamma=None):
+    """K7 over ``trials`` fresh paths of the solver's stream: returns the
+    float64 tensor (sum G, sum G^2, n, sum P, sum P^2, mean G, var G, status)."""
+    from . import kernels as K
+    (f, dim, _), = kernel_models(models)
+    dev = N.require_cuda()
+    cv = _gpu_state(f, dim, dev)
+    inst = solver.lower(payoff, discounter, num_paths=int(trials))
+    return K.price_cv(inst, cv.params, disc_rate(discounter), gamma=gamma)
