@@ -2,9 +2,9 @@
 """Benchmark: prices/s and p50/p99 latency of the served stream, served form
 (continuous batching + control variate) against the plain method.
 
-Headline workload (BASELINE config 5): pricing requests arrive as a Poisson
+Headline workload (the served stream): pricing requests arrive as a Poisson
 process at 2000 req/s (numpy default_rng(1) exponential gaps); each request
-is a config-3 basket call (d ~ U{1..8}, steps log-U[32, 512], pilot paths =
+is a basket call from the mix law (d ~ U{1..8}, steps log-U[32, 512], pilot paths =
 the instance's path count log-U[2^12, 2^18], K ~ U(0.8, 1.2), sigma_i ~
 U(0.1, 0.4), jump rate ~ U(0.5, 3), rho 0.3, log-jumps N(-0.1, 0.2)) with a
 target relative error drawn from {1e-2, 3e-3, 1e-3}; a request is one run_mc
@@ -19,9 +19,10 @@ windows are released back to back at their arrival times.
   back to the host); latencies are arrival -> result.
 * `plain`: the same stream served by the plain method one request at a time
   (pilot K1 launch + readback, main K1 launch + readback).
-* `c2_plain`: config 2 (2D rainbow at 1e-3 relative error) with K1 — the
+* `rainbow2d_plain`: the 2D rainbow at 1e-3 relative error with K1 — the
   per-path kernel every form shares — and its FP32 roofline.
-* `c2_mlmc`, `batched_mix` (config 3), `cv_learned` (config 4): the other
+* `rainbow2d_mlmc`, `batched_mix` (the 512-instance basket mix), `cv_learned`
+  (the learned control variate on the 2D rainbow): the other
   forms, measured once.
 `--impl reference` prices the same stream's requests with the CPU
 restatement of the reference's algorithm (oracle port) on all host cores.
@@ -43,14 +44,14 @@ METRIC = "prices/s and p50/p99 latency at 1e-3 rel. error: CV+batched+served vs 
 UNIT = "prices/s"
 RATE = 2000.0
 WINDOW_S = 0.1
-WORKLOAD = ("config-5 served stream: Poisson arrivals at 2000 req/s (default_rng(1) exponential gaps), each a "
-            "config-3 basket call (d~U{1..8}, steps log-U[32,512], pilot paths log-U[2^12,2^18], K~U(0.8,1.2), "
+WORKLOAD = ("served stream: Poisson arrivals at 2000 req/s (default_rng(1) exponential gaps), each a "
+            "basket call from the mix law (d~U{1..8}, steps log-U[32,512], pilot paths log-U[2^12,2^18], K~U(0.8,1.2), "
             "sigma_i~U(0.1,0.4), jump rate~U(0.5,3), rho 0.3, logN(-0.1,0.2) jumps, r 0.02, T 1) with target "
             "relative error from {1e-2,3e-3,1e-3}; one step = the requests of one 0.1 s window of the stream")
-C2_WORKLOAD = ("config-2 2D rainbow (call on max), Merton assets with independent per-asset jumps "
+RAINBOW_WORKLOAD = ("2D rainbow (call on max), Merton assets with independent per-asset jumps "
                "(rate 1.0, logN(-0.05,0.15)), sigma (0.2,0.3), rho 0.5, r 0.02, T 1, K 1, 256 jump-adapted steps; "
                "one price = plain MC at 1e-3 relative 95% half-width")
-MIX_WORKLOAD = ("config-3 mix: 512 correlated Merton basket calls, d~U{1..8}, steps log-U[32,512], "
+MIX_WORKLOAD = ("basket mix: 512 correlated Merton basket calls, d~U{1..8}, steps log-U[32,512], "
                 "paths log-U[2^12,2^18], K~U(0.8,1.2), sigma_i~U(0.1,0.4), rate~U(0.5,3), rho 0.3, "
                 "logN(-0.1,0.2) jumps; numpy default_rng(0)")
 
@@ -64,12 +65,15 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--plain-windows", type=int, default=10,
                     help="windows of the stream the plain one-request-per-launch server replays")
-    ap.add_argument("--sections", default="c2,mlmc,mix,cv",
-                    help="extra sections measured once: c2, mlmc, mix, cv (comma list, or 'none')")
+    ap.add_argument("--sections", default="rainbow,mlmc,mix,cv",
+                    help="extra sections measured once: rainbow, mlmc, mix, cv (comma list, or 'none')")
     ap.add_argument("--profile-paths", type=int, default=0,
-                    help="profiling driver: three config-2 price launches at this many paths, then exit")
+                    help="profiling driver: three 2D-rainbow price launches at this many paths, then exit")
     ap.add_argument("--profile-serve", type=float, default=0.0,
                     help="profiling driver: serve this many seconds of the stream, then exit")
+    ap.add_argument("--profile-cv", type=int, default=0,
+                    help="profiling driver: K7 over this many 2D-rainbow paths and K5 (tcgen05) over a quarter "
+                         "of them materialised, three launches each, then exit")
     return ap.parse_args()
 
 
@@ -251,8 +255,8 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------ sections ----
-def bench_c2_plain(dev, steps, warmup, fp32_peak):
-    """Config 2 at 1e-3 relative error with K1 (+K10), device-timed, L2
+def bench_rainbow_plain(dev, steps, warmup, fp32_peak):
+    """The 2D rainbow at 1e-3 relative error with K1 (+K10), device-timed, L2
     flushed between steps; the FP32 roofline of price_kernel<2>."""
     import ctypes
     import torch
@@ -302,7 +306,7 @@ def bench_c2_plain(dev, steps, warmup, fp32_peak):
     r_ms = [e[1].elapsed_time(e[2]) for e in evs]
     rows = [r.cpu().tolist() for r in res]
     for r in rows:
-        N.status_error(r[5], "bench c2")
+        N.status_error(r[5], "bench rainbow2d")
     e2e = []
     for i in range(warmup + min(steps, 10)):
         torch.cuda.synchronize()
@@ -313,7 +317,7 @@ def bench_c2_plain(dev, steps, warmup, fp32_peak):
     kernel_s = statistics.mean(k_ms) * 1e-3
     achieved = flops / kernel_s / 1e12
     traffic = (load_json_file(os.path.join("profiles", "kernel_traffic.json")) or {}).get("price_kernel<2,diag>")
-    return {"workload": C2_WORKLOAD, "paths_per_price": n_target, "steps_per_path": steps_per_path,
+    return {"workload": RAINBOW_WORKLOAD, "paths_per_price": n_target, "steps_per_path": steps_per_path,
             "prices_per_s": steps / (sum(k_ms) + sum(r_ms)) * 1e3, "ms_per_price": statistics.mean(
                 [a + b for a, b in zip(k_ms, r_ms)]),
             "e2e_prices_per_s": len(e2e) / sum(e2e), "price": statistics.mean(r[3] for r in rows),
@@ -330,8 +334,8 @@ def bench_c2_plain(dev, steps, warmup, fp32_peak):
             "l2": "flushed (256 MB write) between timed steps", "gpu_launches": 2 * steps}
 
 
-def bench_c2_mlmc(dev):
-    """Config 2 with MLMC (levels 0..6, 2^(l+2) steps) at eps = 1e-3 x price:
+def bench_rainbow_mlmc(dev):
+    """The 2D rainbow with MLMC (levels 0..6, 2^(l+2) steps) at eps = 1e-3 x price:
     Giles' allocation from a 2^14-path pilot per level, then one run."""
     import torch
     import sde_mc_gb300 as sm
@@ -354,11 +358,11 @@ def bench_c2_mlmc(dev):
     return {"levels": levels, "trials": trials, "eps": eps, "price": st.sample_mean,
             "halfwidth": 1.96 * st.sample_std, "prices_per_s": 1.0 / run_s,
             "prices_per_s_with_pilot": 1.0 / (run_s + t_pilot), "path_steps_fine_equiv": fine_steps,
-            "note": "MLMC estimates E[P_L] at L = 256 steps (level 6); plain c2 prices the same target"}
+            "note": "MLMC estimates E[P_L] at L = 256 steps (level 6); the plain rainbow2d section prices the same target"}
 
 
 def bench_batched_mix(steps, warmup):
-    """Config 3: the whole mix per step, batched (K8, autotuned, CUDA graph)
+    """The basket mix: the whole mix per step, batched (K8, autotuned, CUDA graph)
     against the plain method one request per launch (K1 + K10 each)."""
     import torch
     from sde_mc_gb300 import batch as B
@@ -415,7 +419,7 @@ def bench_batched_mix(steps, warmup):
 
 
 def bench_cv_learned(dev, epochs=10):
-    """Config 4: the learned control variate on the config-2 model — train
+    """The learned control variate on the 2D rainbow model — train
     Mlp(3, [64, 64, 64], 2) with Adam (lr 1e-3, batch 4096) on 2^18 paths the
     solver generates (K4 + K5/K6), evaluate on 2^22 fresh paths (K4 + K5);
     VRF against the plain estimator on the same fresh paths and the bias."""
@@ -466,7 +470,7 @@ def bench_cv_learned(dev, epochs=10):
             srv.submit(solver, payoff, disc, rel_target=1e-3, pilot_paths=1 << 18, estimator=est, tag=tag,
                        stream_id=1000)
         reg = {r.tag: r for r in srv.wait(2)}
-    return {"workload": "config-4 learned CV on the config-2 model, Mlp(3,[64,64,64],2) ReLU no BN, Adam lr 1e-3 "
+    return {"workload": "learned CV on the 2D rainbow model, Mlp(3,[64,64,64],2) ReLU no BN, Adam lr 1e-3 "
                         "batch 4096, %d epochs on 2^18 solver paths, evaluated on 2^22 fresh paths" % epochs,
             "vrf": vrf, "mean_cv": st_cv.sample_mean, "se_cv": st_cv.sample_std, "mean_plain": mean_p,
             "se_plain": se_p, "bias": bias, "bias_in_se": bias / math.hypot(st_cv.sample_std, se_p),
@@ -543,6 +547,27 @@ def profile_serve(seconds):
     print(json.dumps(summ))
 
 
+def profile_cv(n):
+    import torch
+    import sde_mc_gb300 as sm
+    from sde_mc_gb300 import kernels as K
+    from sde_mc_gb300 import varred as V
+    solver, payoff, disc = make_problem()
+    dev = torch.device("cuda")
+    torch.manual_seed(0)
+    f = sm.Mlp(3, [64, 64, 64], 2, batch_norm=False, batch_norm_init=False)
+    cv = V.GpuCv(f, 2, dev)
+    for i in range(3):
+        r = K.price_cv(solver.lower(payoff, disc, num_paths=n), cv.params, 0.02)
+    dl = sm.simulate_adapted_data(n // 4, solver, payoff, disc, bs=n // 4, inference=True)
+    data = V.CvData.from_dataset(dl.dataset, solver, dev)
+    for i in range(3):
+        g = cv.forward_tc(data, 0.02)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_cv": n, "k7": r.cpu().tolist(), "tc_status": int(cv._tc_status.item()),
+                      "tc_mean": float(g.double().mean())}))
+
+
 def profile_launches(n):
     import torch
     from sde_mc_gb300 import kernels as K
@@ -569,6 +594,8 @@ def main():
         return profile_launches(args.profile_paths)
     if args.profile_serve:
         return profile_serve(args.profile_serve)
+    if args.profile_cv:
+        return profile_cv(args.profile_cv)
     import torch
     import torch.distributed as dist
     rank, world, local = dist_env()
@@ -635,10 +662,10 @@ def main():
     if rank == 0:
         line["clocks"] = clk.summary()
         secs = [s.strip() for s in args.sections.split(",") if s.strip() and s.strip() != "none"]
-        if "c2" in secs:
-            line["c2_plain"] = _section(bench_c2_plain, dev, 20, 5, fp32_peak)
+        if "rainbow" in secs:
+            line["rainbow2d_plain"] = _section(bench_rainbow_plain, dev, 20, 5, fp32_peak)
         if "mlmc" in secs:
-            line["c2_mlmc"] = _section(bench_c2_mlmc, dev)
+            line["rainbow2d_mlmc"] = _section(bench_rainbow_mlmc, dev)
         if "mix" in secs:
             line["batched_mix"] = _section(bench_batched_mix, 5, 3)
         if "cv" in secs:

@@ -1,7 +1,7 @@
-"""Served-stream workload (config 5) and its two GPU servers.
+"""The served-stream workload and its two GPU servers.
 
 Requests arrive as a Poisson process (exponential gaps from numpy's
-default_rng(seed)); each is a config-3 basket call (d ~ U{1..8}, steps
+default_rng(seed)); each is a basket call from the mix law (d ~ U{1..8}, steps
 log-U[32, 512], pilot paths = the instance's path count log-U[2^12, 2^18],
 K ~ U(0.8, 1.2), sigma_i ~ U(0.1, 0.4), jump rate ~ U(0.5, 3), rho = 0.3,
 log-jumps N(-0.1, 0.2), S0 = 1, r = 0.02, T = 1) with a target relative

@@ -1,9 +1,9 @@
 """Synthetic workloads of the benchmark configurations (no dataset exists for
 this path; instances are drawn from seeded generators with the stated laws).
 
-* :func:`rainbow2d` — config 2: call on the max of two Merton assets with
+* :func:`rainbow2d` — call on the max of two Merton assets with
   independent per-asset jumps.
-* :func:`basket_mix` — config 3: 512 correlated d-dimensional Merton basket
+* :func:`basket_mix` — 512 correlated d-dimensional Merton basket
   calls, d ~ U{1..8}, steps = round(exp(U(ln 32, ln 512))), paths =
   round(2^U(12, 18)), K ~ U(0.8, 1.2), sigma_i ~ U(0.1, 0.4), rate ~
   U(0.5, 3), drawn in that order per instance from numpy's default_rng(seed);

@@ -21,7 +21,7 @@ def merton2d_corr(steps=50, exact=False, seed=1):
 
 
 def indep2d(steps=64, seed=1):
-    """BASELINE config 2 model: per-asset independent jumps, rho = 0.5."""
+    """The 2D rainbow model: per-asset independent jumps, rho = 0.5."""
     corr = sm.get_corr_matrix([0.5])
     m = sm.IndependentJumpsMerton(0.02, torch.tensor([0.2, 0.3]), [1.0, 1.0], -0.05, 0.15, torch.ones(2), 2,
                                   corr_matrix=corr)

@@ -231,7 +231,7 @@ def test_batch_plan_groups_and_orders():
 
 
 def test_basket_mix_law():
-    """Config-3 instance distribution: ranges and the stated draw order."""
+    """The basket-mix instance law: ranges and the stated draw order."""
     from sde_mc_gb300 import workloads
     mix = workloads.basket_mix(512, device="cpu")
     dims = [m.dim for m in mix]

@@ -128,7 +128,7 @@ def test_one_dimensional_network_and_index_gather(oracle_mod):
 
 
 def test_training_reduces_variance_without_bias():
-    """Config-4 set-up at reduced size: the rainbow on two assets with
+    """The learned-CV set-up at reduced size: the rainbow on two assets with
     independent per-asset jumps.  Train on paths the solver generates, then
     price fresh paths with and without the control variate: the variance
     falls and the two means agree within 3 standard errors."""

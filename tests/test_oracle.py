@@ -152,7 +152,7 @@ def test_cv_mixed_precision_restatement_vs_reference(oracle_mod):
 
 
 def test_native_price_vs_merton_closed_form(oracle_mod, kat, ref_stats):
-    """The oracle's own Philox draws through the reference loop price config 1
+    """The oracle's own Philox draws through the reference loop price the 1D Merton call
     within 3 standard errors of the Merton series and of the reference's run."""
     case = merton1d(100)
     inst = inst_for(case, num_paths=1 << 17, seed=11)
