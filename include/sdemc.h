@@ -109,7 +109,7 @@ typedef struct sdemc_inst {
   int32_t payoff_log;   /* Option.log: exp() the state before the payoff    */
   int32_t flags;        /* SDEMC_INST_* bits                                */
   uint32_t stream_id;   /* RNG substream (MLMC level, request id ...)       */
-  uint32_t reserved0;
+  uint32_t model;       /* SDEMC_MODEL_*                                    */
   uint64_t seed;        /* RNG key                                          */
   uint64_t path_offset; /* global index of this instance's first path      */
   int64_t num_paths;
@@ -130,8 +130,27 @@ typedef struct sdemc_inst {
   float chol[SDEMC_CHOL_LEN];     /* Cholesky factor of corr, packed rows     */
   float mark_p[SDEMC_MARK_PARAMS];/* LOGNORMAL: alpha, gamma.
                                      INVCDF: cm, cp, mu, alpha, eps, lda,
-                                     y1, y2, y3, uniform_shift              */
+                                     y1, y2, y3, uniform_shift.
+                                     MODEL_HESTON (no marks): kappa,
+                                     kappa*theta, xi, xi^2                  */
 } sdemc_inst;
+
+/* sdemc_inst.model: how the Euler step reads the coefficients.
+   AFFINE: x_i += (a_i + b_i x_i) dt + (s_i + q_i x_i) dW_i (+ second
+           Brownian for the 'indep' pairs), every Sde class of sde_mc/sde.py
+           except the two below.
+   HESTON: dim 2 (price, variance), HestonScheme.step (sde_mc/schemes.py:16-22,
+           sde_mc/sde.py:258-279): the price takes an Euler step with drift
+           r S (r = drift_b[0]) and diffusion sqrt(v) S; sqrt of the new
+           variance is the larger root of a v'^2 + b v' + c = 0 with
+           a = -1 - kappa h, b = xi dW_1, c = v + kappa theta h - h xi^2 / 2.
+   ASIAN:  dim 2, AsianWrapper (sde_mc/sde.py:378-406) around a 1-D affine
+           model in component 0; component 1 integrates it: y += x_0 dt. */
+enum {
+  SDEMC_MODEL_AFFINE = 0,
+  SDEMC_MODEL_HESTON = 1,
+  SDEMC_MODEL_ASIAN = 2
+};
 
 /* Launch tuning; all-zero means "choose for me". */
 typedef struct sdemc_cfg {

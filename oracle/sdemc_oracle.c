@@ -225,10 +225,42 @@ static float draws_jump_next(const sdemc_inst* I, int D, draws_t* d, float nj) {
 }
 
 /* ------------------------------------------------------------- scheme --- */
+/* HestonScheme.step (sde_mc/schemes.py:16-22): Euler price step, then the
+   larger root of Heston.quadratic_parameters (sde_mc/sde.py:275-279) by
+   solve_quadratic (sde_mc/helpers.py:36-48) squared.  Same float32 order in
+   both Euler modes. */
+static void heston_step(const sdemc_inst* I, float* x, float dt, const float* dW) {
+  float S = x[0], v = x[1];
+  float dr = I->drift_b[0] * S;
+  float sg = sqrtf(v) * S;
+  float base = S + dr * dt;
+  x[0] = base + sg * dW[0];
+  float a = -1.0f - I->mark_p[0] * dt;
+  float b = I->mark_p[2] * dW[1];
+  float c0 = v + I->mark_p[1] * dt;
+  float c = c0 - (0.5f * dt) * I->mark_p[3];
+  float bb = b * b;
+  float a4 = 4.0f * a;
+  float sq = sqrtf(bb - a4 * c);
+  float a2 = 2.0f * a;
+  float r1 = (-b + sq) / a2;
+  float r2 = (-b - sq) / a2;
+  float y = fmaxf(r1, r2);
+  x[1] = y * y;
+}
+
 static void euler(const sdemc_inst* I, int D, int exact, float* x, float dt, const float* dW,
                   const float* dW2) {
+  if (D == 2 && I->model == SDEMC_MODEL_HESTON) { heston_step(I, x, dt, dW); return; }
+  int asian = D == 2 && I->model == SDEMC_MODEL_ASIAN;
+  float x0_old = x[0];
   for (int i = 0; i < D; ++i) {
     float xi = x[i];
+    if (asian && i == 1) {
+      /* AsianWrapper's integral component (sde_mc/sde.py:390-397) */
+      x[1] = exact ? xi + x0_old * dt : fmaf(x0_old, dt, xi);
+      continue;
+    }
     if (exact) {
       float dr = I->drift_a[i] + I->drift_b[i] * xi;
       float sg = I->diff_s[i] + I->diff_q[i] * xi;

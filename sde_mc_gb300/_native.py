@@ -26,6 +26,7 @@ NOISE_DIAG, NOISE_INDEP_SHARED, NOISE_INDEP_PAIR = 0, 1, 2
 GRID_ADAPTED, GRID_UNIFORM = 0, 1
 MARK_NONE, MARK_LOGNORMAL, MARK_INVCDF = 0, 1, 2
 JUMP_COMMON, JUMP_ONE_ASSET = 0, 1
+MODEL_AFFINE, MODEL_HESTON, MODEL_ASIAN = 0, 1, 2
 (PAYOFF_EUROCALL, PAYOFF_EUROPUT, PAYOFF_BINARY_AON, PAYOFF_BASKET_ARITH, PAYOFF_BASKET_GEO,
  PAYOFF_RAINBOW, PAYOFF_DIGITAL, PAYOFF_BESTOF, PAYOFF_ASIANCALL, PAYOFF_HESTON_RAINBOW) = range(10)
 CFG_EXACT_EULER = 1
@@ -39,7 +40,7 @@ class SdemcInst(ctypes.Structure):
         ("dim", ctypes.c_int32), ("noise", ctypes.c_int32), ("grid", ctypes.c_int32),
         ("num_steps", ctypes.c_int32), ("mark", ctypes.c_int32), ("jump_target", ctypes.c_int32),
         ("exact_jumps", ctypes.c_int32), ("payoff", ctypes.c_int32), ("payoff_log", ctypes.c_int32),
-        ("flags", ctypes.c_int32), ("stream_id", ctypes.c_uint32), ("reserved0", ctypes.c_uint32),
+        ("flags", ctypes.c_int32), ("stream_id", ctypes.c_uint32), ("model", ctypes.c_uint32),
         ("seed", ctypes.c_uint64), ("path_offset", ctypes.c_uint64), ("num_paths", ctypes.c_int64),
         ("T", ctypes.c_float), ("h", ctypes.c_float), ("rate", ctypes.c_float),
         ("inv_rate", ctypes.c_float), ("strike", ctypes.c_float), ("payoff_scale", ctypes.c_float),

@@ -56,6 +56,12 @@ int validate_inst(const sdemc_inst* I) {
   if (I->grid == SDEMC_GRID_UNIFORM && I->rate > 0.f) return fail(SDEMC_EUNSUPPORTED, "uniform grid with jumps");
   if (I->payoff < SDEMC_PAYOFF_EUROCALL || I->payoff > SDEMC_PAYOFF_HESTON_RAINBOW) return fail(SDEMC_EUNSUPPORTED, "payoff %d unknown", I->payoff);
   if (I->noise == SDEMC_NOISE_INDEP_PAIR && I->grid != SDEMC_GRID_UNIFORM) return fail(SDEMC_EUNSUPPORTED, "paired noise only on the uniform grid");
+  if (I->model > SDEMC_MODEL_ASIAN) return fail(SDEMC_EINVAL, "model %u unknown", I->model);
+  if (I->model != SDEMC_MODEL_AFFINE && (I->dim != 2 || I->noise != SDEMC_NOISE_DIAG))
+    return fail(SDEMC_EUNSUPPORTED, "Heston and Asian models are 2-D with 'diag' noise");
+  if (I->model == SDEMC_MODEL_HESTON && I->rate > 0.f) return fail(SDEMC_EUNSUPPORTED, "Heston has no jumps");
+  if (I->model == SDEMC_MODEL_ASIAN && I->jump_target != SDEMC_JUMP_COMMON)
+    return fail(SDEMC_EUNSUPPORTED, "the Asian integral takes common jumps only");
   return SDEMC_OK;
 }
 
@@ -187,7 +193,7 @@ int sdemc_inst_offsets(size_t* h_offsets, int* n) {
       offsetof(sdemc_inst, dim), offsetof(sdemc_inst, noise), offsetof(sdemc_inst, grid),
       offsetof(sdemc_inst, num_steps), offsetof(sdemc_inst, mark), offsetof(sdemc_inst, jump_target),
       offsetof(sdemc_inst, exact_jumps), offsetof(sdemc_inst, payoff), offsetof(sdemc_inst, payoff_log),
-      offsetof(sdemc_inst, flags), offsetof(sdemc_inst, stream_id), offsetof(sdemc_inst, reserved0),
+      offsetof(sdemc_inst, flags), offsetof(sdemc_inst, stream_id), offsetof(sdemc_inst, model),
       offsetof(sdemc_inst, seed), offsetof(sdemc_inst, path_offset), offsetof(sdemc_inst, num_paths),
       offsetof(sdemc_inst, T), offsetof(sdemc_inst, h), offsetof(sdemc_inst, rate),
       offsetof(sdemc_inst, inv_rate), offsetof(sdemc_inst, strike), offsetof(sdemc_inst, payoff_scale),

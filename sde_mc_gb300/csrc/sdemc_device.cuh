@@ -380,14 +380,47 @@ struct ReplayDraws {
 };
 
 // ------------------------------------------------------------- scheme -----
+// HestonScheme.step (sde_mc/schemes.py:16-22) with Heston's coefficients
+// (sde_mc/sde.py:269-279) and solve_quadratic (sde_mc/helpers.py:36-48), in
+// the reference's float32 operation order in both Euler modes:
+//   S' = S + (r S) h + (sqrt(v) S) dW_0
+//   a = -1 - kappa h, b = xi dW_1, c = (v + (kappa theta) h) - (0.5 h) xi^2
+//   y = max((-b + sqrt(b b - (4 a) c)) / (2 a), (-b - sqrt(..)) / (2 a)),  v' = y y
+// Under the Feller condition (asserted by Heston) c > 0 and a < 0, so the
+// discriminant is positive.
+SDEMC_DI void heston_step(const sdemc_inst& I, float* x, float dt, const float* dW) {
+  const float S = x[0], v = x[1];
+  const float dr = __fmul_rn(I.drift_b[0], S);
+  const float sg = __fmul_rn(__fsqrt_rn(v), S);
+  x[0] = __fadd_rn(__fadd_rn(S, __fmul_rn(dr, dt)), __fmul_rn(sg, dW[0]));
+  const float a = __fsub_rn(-1.f, __fmul_rn(I.mark_p[0], dt));
+  const float b = __fmul_rn(I.mark_p[2], dW[1]);
+  const float c = __fsub_rn(__fadd_rn(v, __fmul_rn(I.mark_p[1], dt)), __fmul_rn(__fmul_rn(0.5f, dt), I.mark_p[3]));
+  const float sq = __fsqrt_rn(__fsub_rn(__fmul_rn(b, b), __fmul_rn(__fmul_rn(4.f, a), c)));
+  const float a2 = __fmul_rn(2.f, a);
+  const float r1 = __fdiv_rn(__fadd_rn(-b, sq), a2);
+  const float r2 = __fdiv_rn(__fsub_rn(-b, sq), a2);
+  const float y = fmaxf(r1, r2);
+  x[1] = __fmul_rn(y, y);
+}
+
 // EulerScheme.step (sde_mc/schemes.py:7-10) for the affine coefficient form.
 // EXACT: the reference's unfused float32 order  x + drift*h + diffusion*dW.
 // fast : a fixed chain of fused multiply-adds (mirrored by the oracle).
+// MODEL_ASIAN: component 1 is AsianWrapper's running integral
+// (sde_mc/sde.py:390-397): y + x_0 h + 0 dW_1, x_0 taken before the step.
 template <int D, int NOISE, bool EXACT>
 SDEMC_DI void euler(const sdemc_inst& I, float* x, float dt, const float* dW, const float* dW2) {
+  if (D == 2 && I.model == SDEMC_MODEL_HESTON) { heston_step(I, x, dt, dW); return; }
+  const bool asian = D == 2 && I.model == SDEMC_MODEL_ASIAN;
+  const float x0_old = x[0];
 #pragma unroll
   for (int i = 0; i < D; ++i) {
     const float xi = x[i];
+    if (D == 2 && i == 1 && asian) {
+      x[1] = EXACT ? __fadd_rn(xi, __fmul_rn(x0_old, dt)) : __fmaf_rn(x0_old, dt, xi);
+      continue;
+    }
     if (EXACT) {
       const float dr = __fadd_rn(I.drift_a[i], __fmul_rn(I.drift_b[i], xi));
       const float sg = __fadd_rn(I.diff_s[i], __fmul_rn(I.diff_q[i], xi));

@@ -107,6 +107,8 @@ CvWeights cv_weights(const sdemc_inst& I) {
     for (int j = 0; j <= i; ++j) L[i][j] = I.chol[q++];
   double sig[SDEMC_MAX_DIM];
   for (int i = 0; i < d; ++i) sig[i] = std::fabs((double)I.diff_q[i]);
+  // Heston's price volatility is sqrt(v): weight with the initial variance's
+  if (I.model == SDEMC_MODEL_HESTON) sig[0] = std::sqrt(std::max((double)I.x0[1], 0.0));
   double var = 0.0;
   if (cw.agg == 0) {
     var = sig[0] * sig[0];

@@ -56,6 +56,7 @@ def lower_sde(sde, inst):
     name = _name(sde)
     zero, one = [0.0] * d, [1.0] * d
     inst.noise = N.NOISE_DIAG
+    inst.model = N.MODEL_AFFINE
     inst.mark = N.MARK_NONE
     inst.jump_target = N.JUMP_COMMON
     inst.rate = 0.0
@@ -101,10 +102,32 @@ def lower_sde(sde, inst):
         _set(inst.diff2_q, _vec(sde.sigma2, d))
     elif name == "LevySde":
         lower_levy(sde, inst, d)
+    elif name == "Heston":
+        # sde_mc/sde.py:258-279: drift (r S, 0), diffusion (sqrt(v) S, 0) and
+        # the quadratic's coefficients as torch forms them from Python floats:
+        # kappa*h, (kappa*theta)*h, xi*dW, (0.5*h)*(xi**2)
+        inst.model = N.MODEL_HESTON
+        _set(inst.drift_b, [_f32(sde.r), 0.0])
+        k, th, xi = float(sde.kappa), float(sde.theta), float(sde.xi)
+        _set(inst.mark_p, [_f32(k), _f32(k * th), _f32(xi), _f32(xi ** 2)] + [0.0] * (N.MARK_PARAMS - 4))
+    elif name == "AsianWrapper":
+        # sde_mc/sde.py:378-406: a 1-D model in component 0, its time
+        # integral in component 1 (no diffusion, no jumps)
+        base = sde.base_sde
+        if int(base.dim) != 1:
+            raise NotImplementedError("AsianWrapper lowers around a 1-D model only")
+        sub = lower_sde(base, N.SdemcInst())
+        if sub.model != N.MODEL_AFFINE or sub.noise != N.NOISE_DIAG:
+            raise NotImplementedError("AsianWrapper lowers around an affine 'diag' model only")
+        for f in ("drift_a", "drift_b", "diff_s", "diff_q", "jump_g", "jump_k"):
+            getattr(inst, f)[0] = getattr(sub, f)[0]
+        inst.mark, inst.rate, inst.inv_rate = sub.mark, sub.rate, sub.inv_rate
+        _set(inst.mark_p, list(sub.mark_p))
+        inst.model = N.MODEL_ASIAN
     else:
         raise NotImplementedError(
             "no GPU lowering for Sde class %r (supported: Merton, IndependentJumpsMerton, Gbm, LogGbm, "
-            "DoubleGbm, LevySde over ExpExampleLevy/ExampleLevy/Levy2d)" % name)
+            "DoubleGbm, Heston, AsianWrapper, LevySde over ExpExampleLevy/ExampleLevy/Levy2d)" % name)
     return inst
 
 
@@ -200,8 +223,16 @@ def lower(solver, payoff=None, discounter=None, num_paths=0, path_offset=0, stre
     inst = N.SdemcInst()
     sde = solver.sde
     lower_sde(sde, inst)
-    if _name(solver) in ("HestonSolver",) or getattr(sde, "simulation_method", "euler") == "heston":
-        raise NotImplementedError("the Heston implicit scheme has no GPU kernel yet")
+    heston_scheme = _name(solver) == "HestonSolver"
+    if heston_scheme and inst.model != N.MODEL_HESTON:
+        raise NotImplementedError("HestonSolver steps a Heston model only")
+    if inst.model == N.MODEL_HESTON and not heston_scheme:
+        # EulerScheme on Heston: the variance has zero drift and diffusion, so
+        # it stays at v0 and the price is a GBM with volatility sqrt(v0)
+        inst.model = N.MODEL_AFFINE
+        v0 = np.float32(inst.x0[1])
+        inst.diff_q[0] = float(np.sqrt(v0))
+        inst.mark_p[0] = inst.mark_p[1] = inst.mark_p[2] = inst.mark_p[3] = 0.0
     steps = int(num_steps if num_steps is not None else solver.num_steps)
     T = float(solver.time_interval)
     inst.num_steps = steps

@@ -88,10 +88,8 @@ class EulerSolver(EulerScheme, DiffusionSolver):
 
 
 class HestonSolver(HestonScheme, DiffusionSolver):
-    """Heston's implicit variance scheme has no GPU kernel yet: solve() raises."""
-
-    def solve(self, bs=1, return_normals=False):
-        raise NotImplementedError("the Heston implicit scheme has no GPU kernel yet")
+    """Uniform grid with Heston's implicit variance step (sde_mc/solvers.py:126-127);
+    the kernels run it as the Heston model kind of the descriptor."""
 
 
 class JumpDiffusionSolver(SdeSolver):

@@ -39,6 +39,19 @@ def gbm_uniform(steps=12, seed=1):
     return sm.EulerSolver(g, 1.0, steps, seed=seed), sm.EuroCall(1.0), sm.ConstantShortRate(0.02)
 
 
+def heston(steps=24, seed=1):
+    """Heston (price, variance), rho = -0.7, on the uniform grid."""
+    h = sm.Heston(0.02, 2.0, 0.04, 0.3, -0.7, torch.tensor([1., 0.04]))
+    return sm.HestonSolver(h, 1.0, steps, seed=seed), sm.EuroCall(1.0), sm.ConstantShortRate(0.02)
+
+
+def asian_merton(steps=20, seed=1):
+    """An Asian call on a 1-D Merton (AsianWrapper) on the jump-adapted grid."""
+    m = sm.Merton(0.02, 0.2, 2.0, -0.1, 0.2, torch.tensor([1.]), dim=1)
+    return (sm.JumpEulerSolver(sm.AsianWrapper(m), 1.0, steps, seed=seed), sm.AsianCall(1.0, 1.0),
+            sm.ConstantShortRate(0.02))
+
+
 def basket(d, steps=64, seed=1):
     rho = 0.3
     corr = sm.get_corr_matrix([rho] * (d * (d - 1) // 2)) if d > 1 else None
@@ -59,6 +72,8 @@ FIXTURE_CASES = {
     "replay_indep2d": lambda: indep2d(64),
     "replay_levy2d": lambda: levy2d(16),
     "replay_gbm_uniform": lambda: gbm_uniform(12),
+    "replay_heston": lambda: heston(24),
+    "replay_asian_merton": lambda: asian_merton(20),
 }
 
 

@@ -214,12 +214,56 @@ def cv_jump_fixture(sm, torch):
     np.savez_compressed(os.path.join(HERE, 'cv_mlp_jumps.npz'), **out)
 
 
+def heston_asian_fixtures(sm, torch):
+    """Replay cases for the two non-affine models: Heston with its implicit
+    variance step (sde_mc/schemes.py:16-22, sde.py:258-279) on the uniform
+    grid, and AsianWrapper (sde.py:378-406) around a 1-D Merton on the
+    jump-adapted grid."""
+    cases = {}
+    csr = sm.ConstantShortRate(0.02)
+    h = sm.Heston(0.02, 2.0, 0.04, 0.3, -0.7, torch.tensor([1., 0.04]))
+    sol = sm.HestonSolver(h, 1.0, 24)
+    torch.manual_seed(31)
+    rec = Recorder(sol)
+    hp, _ = sol.solve(bs=16)
+    rec.restore()
+    cases['replay_heston'] = dict(
+        bs=np.int64(16), S=np.int64(24), dw=torch.stack([cn for _, cn in rec.steps], 1).numpy().astype(np.float32),
+        paths=hp.numpy().astype(np.float32), chol=sol.lower_cholesky.numpy().astype(np.float32),
+        payoffs=(sm.EuroCall(1.0)(hp[:, -1]) * csr(1.0)).numpy().astype(np.float32))
+    # DiffusionSolver.multilevel_solve (sde_mc/solvers.py:90-119) through
+    # the Heston scheme: `factor` fine steps, then one coarse step on the
+    # summed increments
+    for name, levels, seed in (('mlmc_heston', (8, 4), 33), ('mlmc_heston_f4', (16, 4), 34)):
+        fine, coarse = levels
+        factor = fine // coarse
+        sol = sm.HestonSolver(h, 1.0, coarse)
+        torch.manual_seed(seed)
+        rec = Recorder(sol)
+        (pf, pc), _ = sol.multilevel_solve(32, levels)
+        rec.restore()
+        fine_calls = [c for i, c in enumerate(rec.steps) if i % (factor + 1) != factor]
+        h_fine = torch.tensor(1.0 / fine)
+        cases[name] = dict(
+            bs=np.int64(32), fine=np.int64(fine), coarse=np.int64(coarse),
+            dw=torch.stack([cn for _, cn in fine_calls], 1).numpy().astype(np.float32),
+            xf=pf[:, -1].numpy().astype(np.float32), xc=pc[:, -1].numpy().astype(np.float32),
+            h_fine=np.float32(h_fine.item()), h_coarse=np.float32((factor * h_fine).item()))
+    m = sm.Merton(0.02, 0.2, 2.0, -0.1, 0.2, torch.tensor([1.]), dim=1)
+    aw = sm.AsianWrapper(m)
+    sol2 = sm.JumpEulerSolver(aw, 1.0, 20)
+    cases['replay_asian_merton'] = jump_replay_case(sm, torch, sol2, 32, sm.AsianCall(1.0, 1.0), csr, seed=32)
+    cases['replay_asian_merton']['chol'] = sol2.lower_cholesky.numpy().astype(np.float32)
+    for name, arrs in cases.items():
+        np.savez_compressed(os.path.join(HERE, name + '.npz'), **{k: np.asarray(v) for k, v in arrs.items()})
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--ref', default='/root/reference')
     ap.add_argument('--skip-stats', action='store_true')
-    ap.add_argument('--only', choices=['cv_jumps'], default=None,
-                    help='write only this fixture')
+    ap.add_argument('--only', choices=['cv_jumps', 'heston_asian'], default=None,
+                    help='write only these fixtures')
     args = ap.parse_args()
     sm = load_reference(args.ref)
     import torch
@@ -228,7 +272,11 @@ def main():
     if args.only == 'cv_jumps':
         cv_jump_fixture(sm, torch)
         return
+    if args.only == 'heston_asian':
+        heston_asian_fixtures(sm, torch)
+        return
     cv_jump_fixture(sm, torch)
+    heston_asian_fixtures(sm, torch)
 
     # ------------------------------------------------------------ KATs ----
     kat = {}

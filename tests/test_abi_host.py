@@ -281,3 +281,24 @@ def test_adapted_path_data_round_trip(tmp_path):
     for x, y in zip(a[0], b[0]):
         assert torch.equal(x, y)
     assert torch.equal(a[1], b[1])
+
+
+def test_heston_and_asian_lowering():
+    from tests.cases import asian_merton, heston
+    f = np.float32
+    inst = inst_for(heston(24), num_paths=4)
+    assert inst.model == N.MODEL_HESTON and inst.grid == N.GRID_UNIFORM and inst.rate == 0.0
+    assert inst.drift_b[0] == f(0.02)
+    assert list(inst.mark_p[:4]) == [f(2.0), f(2.0 * 0.04), f(0.3), f(0.3 ** 2)]
+    a = inst_for(asian_merton(20), num_paths=4)
+    assert a.model == N.MODEL_ASIAN and a.dim == 2 and a.grid == N.GRID_ADAPTED
+    assert list(a.x0[:2]) == [1.0, 0.0] and list(a.jump_k[:2]) == [1.0, 0.0]
+    assert a.drift_b[1] == 0.0 and a.diff_q[1] == 0.0 and a.rate == 2.0 and a.mark == N.MARK_LOGNORMAL
+    assert a.payoff == N.PAYOFF_ASIANCALL
+    # EulerScheme on a Heston model: the variance never moves, the price is a
+    # GBM with volatility sqrt(v0)
+    h = sm.Heston(0.02, 2.0, 0.04, 0.3, -0.7, torch.tensor([1., 0.04]))
+    e = lower(sm.EulerSolver(h, 1.0, 10), sm.EuroCall(1.0), None, num_paths=4)
+    assert e.model == N.MODEL_AFFINE and e.diff_q[0] == np.sqrt(f(0.04)) and e.diff_q[1] == 0.0
+    with pytest.raises(NotImplementedError):
+        lower(sm.HestonSolver(sm.Gbm(0.02, 0.2, torch.ones(2), 2), 1.0, 10), sm.EuroCall(1.0), None)

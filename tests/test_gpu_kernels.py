@@ -17,8 +17,8 @@ import torch
 
 from sde_mc_gb300 import _native as N
 from sde_mc_gb300 import kernels as K
-from tests.cases import (FIXTURE_CASES, basket, double_gbm, gbm_uniform, indep2d, inst_for, levy2d,
-                         merton1d, merton2d_corr, zdim)
+from tests.cases import (FIXTURE_CASES, asian_merton, basket, double_gbm, gbm_uniform, heston, indep2d, inst_for,
+                         levy2d, merton1d, merton2d_corr, zdim)
 from tests.conftest import load_npz
 from tests.test_oracle import expected_jump_paths
 
@@ -46,6 +46,11 @@ def test_replay_matches_reference(name, oracle_mod):
         np.testing.assert_array_equal(np_(out["time"]), fx["time"])
         np.testing.assert_allclose(paths, fx["paths"], rtol=1e-5, atol=1e-6)
         np.testing.assert_allclose(np_(out["payoffs"]), fx["payoffs"], rtol=1e-5, atol=1e-6)
+    elif name == "replay_heston":
+        # correctly rounded sqrt here, torch's x86 CPU sqrt in the fixture:
+        # near-tie roundings differ (pinned step by step in test_oracle.py)
+        np.testing.assert_allclose(paths, fx["paths"], rtol=2e-6, atol=1e-9)
+        np.testing.assert_allclose(np_(out["payoffs"]), fx["payoffs"], rtol=2e-6, atol=1e-9)
     else:
         np.testing.assert_array_equal(paths[:, :S + 1], fx["paths"])
         if "time" in fx:
@@ -58,6 +63,7 @@ def test_replay_matches_reference(name, oracle_mod):
     ref = oracle_mod.replay(inst, fx["dw"], fx.get("jump_times") if inst.grid == 0 else None,
                             fx.get("marks") if inst.grid == 0 else None, fx.get("asset"))
     np.testing.assert_array_equal(paths, ref["paths"])
+    np.testing.assert_array_equal(np_(out["payoffs"]), ref["payoffs"])
 
 
 @pytest.mark.parametrize("name,factory,levels", [("mlmc_merton1d", lambda: merton1d(4), (8, 4)),
@@ -71,6 +77,22 @@ def test_mlmc_replay_matches_reference(name, factory, levels):
                         torch.from_numpy(fx["marks"]), asset)
     assert int(out["status"].item()) == 0
     np.testing.assert_array_equal(np_(out["xf"]), fx["xf"])
+    np.testing.assert_array_equal(np_(out["xc"]), fx["xc"])
+
+
+@pytest.mark.parametrize("name,levels", [("mlmc_heston", (8, 4)), ("mlmc_heston_f4", (16, 4))])
+def test_mlmc_replay_heston(name, levels, oracle_mod):
+    """K2's uniform-grid coupled Heston levels equal the oracle's bit for bit
+    (which pins them to the reference, test_oracle.py)."""
+    fx = load_npz(name)
+    inst = inst_for(heston(levels[1]), num_paths=int(fx["bs"]), steps=levels[1])
+    out = K.mlmc_replay(inst, levels[0], levels[1], float(fx["h_fine"]), float(fx["h_coarse"]),
+                        torch.from_numpy(fx["dw"]), levels[1])
+    assert int(out["status"].item()) == 0
+    ref = oracle_mod.mlmc_replay(inst, levels[0] // levels[1], float(fx["h_fine"]), float(fx["h_coarse"]),
+                                 fx["dw"], levels[1])
+    np.testing.assert_array_equal(np_(out["xf"]), ref["xf"])
+    np.testing.assert_array_equal(np_(out["xc"]), ref["xc"])
     np.testing.assert_array_equal(np_(out["xc"]), fx["xc"])
 
 
@@ -93,6 +115,8 @@ EXPORT_CASES = {
     "basket5": lambda: basket(5, 24),
     "basket8": lambda: basket(8, 16),
     "double_gbm": lambda: double_gbm(3, 10),
+    "heston": lambda: heston(24),
+    "asian_merton": lambda: asian_merton(20),
 }
 
 
@@ -121,7 +145,7 @@ def test_materialise_matches_oracle_step_by_step(name, oracle_mod):
         np.testing.assert_array_equal(g[key], ref[key], err_msg=key)
 
 
-@pytest.mark.parametrize("name", ["merton1d", "indep2d", "levy2d", "basket5", "double_gbm"])
+@pytest.mark.parametrize("name", ["merton1d", "indep2d", "levy2d", "basket5", "double_gbm", "heston"])
 def test_native_draws_match_oracle_transforms(name, oracle_mod):
     """Philox words are bit-exact (above); the MUFU-based Box-Muller and the
     jump-stream transforms agree with the oracle's libm versions to 2e-5."""
@@ -138,7 +162,8 @@ def test_native_draws_match_oracle_transforms(name, oracle_mod):
             np.testing.assert_array_equal(np_(out["jsel"])[p], js)
 
 
-@pytest.mark.parametrize("name", ["merton1d", "merton2d_corr", "indep2d", "levy2d", "gbm_uniform", "basket8"])
+@pytest.mark.parametrize("name", ["merton1d", "merton2d_corr", "indep2d", "levy2d", "gbm_uniform", "basket8",
+                                  "heston", "asian_merton"])
 def test_fused_price_matches_materialised_and_reduction(name, oracle_mod):
     case = EXPORT_CASES[name]()
     n = 5000

@@ -57,7 +57,7 @@ def _replay(oracle_mod, name):
 
 
 @pytest.mark.parametrize("name", ["replay_merton1d", "replay_merton2d_corr", "replay_merton2d_exact",
-                                  "replay_indep2d", "replay_gbm_uniform"])
+                                  "replay_indep2d", "replay_gbm_uniform", "replay_asian_merton"])
 def test_replay_bit_exact_vs_reference(oracle_mod, name):
     """Recorded reference draws through the oracle's loop give the reference's
     paths, time grid, left limits, jump marks and payoffs bit for bit."""
@@ -70,7 +70,66 @@ def test_replay_bit_exact_vs_reference(oracle_mod, name):
         np.testing.assert_array_equal(out["left"], fx["left"])
         np.testing.assert_array_equal(out["jumps"], expected_jump_paths(fx))
         assert int(out["steps"].max()) == int(fx["S"])
+    if "payoffs" in fx:
         np.testing.assert_array_equal(out["payoffs"], fx["payoffs"])
+
+
+def sqrt_tie_distance(v):
+    """How far sqrt(v) (v float32) lies from the midpoint between its two
+    neighbouring float32 values, in units of their spacing (0 = a tie)."""
+    v = np.asarray(v, np.float32)
+    exact = np.sqrt(v.astype(np.float64))
+    lo = np.sqrt(v).astype(np.float32)
+    lo = np.where(lo.astype(np.float64) > exact, np.nextafter(lo, np.float32(0)), lo)
+    hi = np.nextafter(lo, np.float32(np.inf))
+    frac = (exact - lo.astype(np.float64)) / (hi.astype(np.float64) - lo.astype(np.float64))
+    return np.abs(frac - 0.5)
+
+
+def heston_sqrt_inputs(x, dw1, inst):
+    """The two square-root arguments of one Heston step from state x:
+    v (the price diffusion) and b b - 4 a c (solve_quadratic), in the
+    reference's float32 order (sde_mc/sde.py:275-279, helpers.py:46-47)."""
+    f = np.float32
+    v, h = x[..., 1].astype(f), f(inst.h)
+    kap, kth, xi, xi2 = (f(inst.mark_p[i]) for i in range(4))
+    a = f(-1) - kap * h
+    b = xi * dw1.astype(f)
+    c = (v + kth * h) - (f(0.5) * h) * xi2
+    return v, (b * b) - (f(4) * a) * c
+
+
+def test_replay_heston_vs_reference(oracle_mod):
+    """Heston's implicit variance step (sde_mc/schemes.py:16-22).  The oracle
+    and the kernels take correctly rounded square roots; the fixture was
+    recorded with torch's x86 CPU sqrt, which rounds a near-tie the other way
+    now and then.  So: one step of the oracle from every recorded state gives
+    the recorded next state bit for bit except where a square-root argument
+    sits within 1% of a rounding tie, and the whole trajectories agree to
+    float32 rounding."""
+    fx, inst, out = _replay(oracle_mod, "replay_heston")
+    assert out["rc"] == 0
+    P, dw = fx["paths"], fx["dw"]
+    np.testing.assert_allclose(out["paths"], P, rtol=2e-6, atol=1e-9)
+    np.testing.assert_allclose(out["payoffs"], fx["payoffs"], rtol=2e-6, atol=1e-9)
+    assert np.mean(out["paths"] == P) > 0.99
+    bs, S = dw.shape[0], dw.shape[1]
+    one = inst_for(FIXTURE_CASES["replay_heston"](), num_paths=1)
+    one.num_steps = 1
+    mism, ties = 0, 0
+    for p in range(bs):
+        for k in range(S):
+            for i in range(2):
+                one.x0[i] = float(P[p, k, i])
+            o = oracle_mod.replay(one, dw[p:p + 1, k:k + 1])
+            assert o["rc"] == 0
+            if not np.array_equal(o["paths"][0, 1], P[p, k + 1]):
+                mism += 1
+                v, disc = heston_sqrt_inputs(P[p, k], dw[p, k, 1], inst)
+                near = min(sqrt_tie_distance(v), sqrt_tie_distance(disc))
+                assert near < 0.01, (p, k, o["paths"][0, 1], P[p, k + 1], near)
+                np.testing.assert_allclose(o["paths"][0, 1], P[p, k + 1], rtol=1e-6)
+    assert mism <= 4
 
 
 def expected_jump_paths(fx):
@@ -108,6 +167,27 @@ def test_mlmc_replay_bit_exact(oracle_mod, name, factory, levels):
     assert out["rc"] == 0
     np.testing.assert_array_equal(out["xf"], fx["xf"])
     np.testing.assert_array_equal(out["xc"], fx["xc"])
+
+
+@pytest.mark.parametrize("name,levels,exact", [("mlmc_heston", (8, 4), False), ("mlmc_heston_f4", (16, 4), True)])
+def test_mlmc_replay_heston(oracle_mod, name, levels, exact):
+    """Coupled fine/coarse Heston levels (DiffusionSolver.multilevel_solve,
+    sde_mc/solvers.py:90-119): the coarse step takes the fine increments'
+    sum in the reference's order.  Bit-exact except where torch's x86 CPU
+    sqrt rounded a near-tie the other way (one path of 32 in the (8, 4)
+    fixture); those agree to float32 rounding."""
+    from tests.cases import heston
+    fx = load_npz(name)
+    inst = inst_for(heston(levels[1]), num_paths=int(fx["bs"]), steps=levels[1])
+    out = oracle_mod.mlmc_replay(inst, levels[0] // levels[1], float(fx["h_fine"]), float(fx["h_coarse"]),
+                                 fx["dw"], levels[1])
+    assert out["rc"] == 0
+    np.testing.assert_array_equal(out["xc"], fx["xc"])
+    if exact:
+        np.testing.assert_array_equal(out["xf"], fx["xf"])
+    else:
+        np.testing.assert_allclose(out["xf"], fx["xf"], rtol=2e-6)
+        assert np.all(out["xf"] == fx["xf"], axis=1).sum() >= int(fx["bs"]) - 1
 
 
 def test_cv_mlp_grads_and_adam(oracle_mod):
