@@ -65,8 +65,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--plain-windows", type=int, default=10,
                     help="windows of the stream the plain one-request-per-launch server replays")
-    ap.add_argument("--sections", default="rainbow,mlmc,mix,cv",
-                    help="extra sections measured once: rainbow, mlmc, mix, cv (comma list, or 'none')")
+    ap.add_argument("--sections", default="rainbow,mlmc,mix,cv,accuracy",
+                    help="extra sections measured once: rainbow, mlmc, mix, cv, accuracy (comma list, "
+                         "or 'none')")
     ap.add_argument("--profile-paths", type=int, default=0,
                     help="profiling driver: three 2D-rainbow price launches at this many paths, then exit")
     ap.add_argument("--profile-serve", type=float, default=0.0,
@@ -486,6 +487,94 @@ def bench_cv_learned(dev, epochs=10):
                     "simulates the paths inside the same kernel (nothing materialised)"}
 
 
+def _err(mean, se, ref, ref_se):
+    e = mean - ref
+    return {"price": mean, "err": e, "rel_err": e / ref, "err_in_se": e / math.hypot(se, ref_se)}
+
+
+def bench_accuracy(dev, line, served):
+    """Every price of the bench against an FP64 oracle: the Merton series for
+    the 1-D Merton call; for the 2D rainbow (no closed form) a 2^26-path run
+    of K11, which repeats the path arithmetic in FP64; for the served stream a
+    sample of requests, each against its own K11 run on fresh paths.  K11 on
+    the same paths as an FP32 run isolates the FP32 arithmetic's error."""
+    import torch
+    import sde_mc_gb300 as sm
+    from sde_mc_gb300 import _native as N
+    from sde_mc_gb300 import kernels as K
+    from sde_mc_gb300.lowering import lower
+    out = {}
+    # the 1-D Merton call (100 steps, 2^16 paths)
+    m = sm.Merton(0.02, 0.2, 2.0, -0.1, 0.2, torch.tensor([1.]), dim=1)
+    inst = lower(sm.JumpEulerSolver(m, 1.0, 100, seed=1), sm.EuroCall(1.0), sm.ConstantShortRate(0.02),
+                 num_paths=1 << 16)
+    a, b = K.price(inst).cpu().tolist(), K.price_f64(inst).cpu().tolist()
+    series = sm.merton_call(1.0, 1.0, 1.0, 0.02, 0.2, -0.1, 0.2, 2.0)
+    out["merton1d"] = {"workload": "1-D Merton call, 100 jump-adapted steps, 2^16 paths",
+                       "oracle": "Merton series (FP64)", "oracle_value": series,
+                       "fp32": _err(a[3], math.sqrt(a[4] / a[2]), series, 0.0),
+                       "fp64_same_paths": _err(b[3], math.sqrt(b[4] / b[2]), series, 0.0),
+                       "fp32_minus_fp64_same_paths_rel": (a[3] - b[3]) / b[3]}
+    # the 2D rainbow: FP64 reference run on 2^26 paths
+    solver, payoff, disc = make_problem()
+    n_ref = 1 << 26
+    ref_inst = lower(solver, payoff, disc, num_paths=n_ref, path_offset=1 << 44, seed=99)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r = K.price_f64(ref_inst).cpu().tolist()
+    t_ref = time.perf_counter() - t0
+    N.status_error(r[5], "fp64 reference")
+    ref, ref_se = r[3], math.sqrt(r[4] / r[2])
+    rb = {"workload": RAINBOW_WORKLOAD, "oracle": "K11 FP64 run, 2^26 paths", "oracle_value": ref,
+          "oracle_se": ref_se, "oracle_s": t_ref, "fp64_path_steps_per_s": None}
+    plain = line.get("rainbow2d_plain") or {}
+    if "price" in plain:
+        n = plain["paths_per_price"]
+        se = plain["rel_halfwidth"] * plain["price"] / 1.96
+        rb["plain_fp32"] = _err(plain["price"], se, ref, ref_se)
+        same = lower(solver, payoff, disc, num_paths=n, path_offset=n, seed=1)
+        a, b = K.price(same).cpu().tolist(), K.price_f64(same).cpu().tolist()
+        rb["fp32_minus_fp64_same_paths_rel"] = (a[3] - b[3]) / b[3]
+        rb["fp32_minus_fp64_same_paths_in_se"] = (a[3] - b[3]) / math.sqrt(b[4] / b[2])
+        rb["fp64_path_steps_per_s"] = n_ref * plain["steps_per_path"] / t_ref
+    ml = line.get("rainbow2d_mlmc") or {}
+    if "price" in ml:
+        rb["mlmc"] = _err(ml["price"], ml["halfwidth"] / 1.96, ref, ref_se)
+    cv = line.get("cv_learned") or {}
+    if "mean_cv" in cv:
+        rb["learned_cv"] = _err(cv["mean_cv"], cv["se_cv"], ref, ref_se)
+        reg = cv.get("regression_cv_same_model") or {}
+        if "mean" in reg:
+            rb["served_regression_cv"] = _err(reg["mean"], reg["se"], ref, ref_se)
+    out["rainbow2d"] = rb
+    # served requests: every k-th timed request against its own FP64 run
+    if served:
+        res, timed = served["results"], served["timed"]
+        step = max(1, len(timed) // 16)
+        rows = []
+        t0 = time.perf_counter()
+        for q in timed[::step][:16]:
+            x = res[q.idx]
+            sd = x.pilot_se * math.sqrt(x.pilot_paths)
+            n_q = int(min(1 << 24, max(1 << 20, 9 * (sd / max(x.se, 1e-300)) ** 2)))
+            rr = K.price_f64(q.phase(n_q, 1 << 44)).cpu().tolist()
+            N.status_error(rr[5], "fp64 served reference")
+            e = _err(x.mean, x.se, rr[3], math.sqrt(rr[4] / rr[2]))
+            e.update(target=q.target, dim=q.dim, fp64_paths=n_q, estimator=x.estimator_name(),
+                     within_target=abs(e["err"]) <= q.target * abs(rr[3]))
+            rows.append(e)
+        out["served_sample"] = {
+            "requests": len(rows), "seconds": time.perf_counter() - t0,
+            "within_target": sum(1 for e in rows if e["within_target"]),
+            "within_1.96_se": sum(1 for e in rows if abs(e["err_in_se"]) <= 1.96),
+            "max_abs_err_in_se": max(abs(e["err_in_se"]) for e in rows),
+            "median_rel_err_over_target": statistics.median(abs(e["rel_err"]) / e["target"] for e in rows),
+            "rows": rows,
+            "note": "each request's price vs a K11 FP64 run of the same instance on fresh paths "
+                    "(2^20..2^24 paths, about a third of the request's standard error)"}
+    return out
+
+
 def shard(reqs, rank, world):
     """Requests of one rank: the stream is partitioned by request index (each
     request is independent; no exchange on the data path)."""
@@ -670,6 +759,8 @@ def main():
             line["batched_mix"] = _section(bench_batched_mix, 5, 3)
         if "cv" in secs:
             line["cv_learned"] = _section(bench_cv_learned, dev)
+        if "accuracy" in secs:
+            line["accuracy"] = _section(bench_accuracy, dev, line, b)
         spr, n, threads, paths = oracle_serve(b["timed"], args.cpu_seconds)
         line["cpu_baseline"] = {"value": 1.0 / spr, "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": "%d requests of the timed stream (pilot + main, plain estimator, %d paths "

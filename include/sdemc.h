@@ -208,6 +208,17 @@ int sdemc_price_chunks(const sdemc_inst* h_inst, const sdemc_cfg* h_cfg,
 int sdemc_reduce_chunks(void* d_scratch, int64_t nchunks, int width,
                         double* d_out, void* stream);
 
+/* K11: the FP64 reference run.  Prices *h_inst with every path operation in
+   double precision (grid, steps, jumps, transforms of the draws, payoff) from
+   the same Philox words sdemc_price uses for the same paths, so the two means
+   differ by the FP32 arithmetic's error alone; with more paths it is the
+   FP64 oracle for payoffs without a closed form.  'diag' noise, no marks or
+   lognormal marks, terminal payoff.  Scratch as sdemc_price_scratch_bytes;
+   d_out receives (sum, sum_sq, n, mean, var, status).  Stands in for no
+   reference function: the reference's own numbers are float32. */
+int sdemc_price_f64(const sdemc_inst* h_inst, void* d_scratch, size_t scratch_bytes,
+                    double* d_out, void* stream);
+
 /* ---- pricing without allocation ----------------------------------------
  * No counterpart in the reference (which has no native code): sdemc_price for
  * callers that cannot allocate device memory — a host that owns all GPU

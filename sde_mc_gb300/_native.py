@@ -91,6 +91,7 @@ _PROTOS = {
                                  ctypes.c_size_t, _P, _P]),
     "sdemc_price_cv_scratch_bytes": (ctypes.c_size_t, [_P]),
     "sdemc_price_cv": (_I, [_P, _P, ctypes.c_float, _P, ctypes.c_size_t, _P, _P, _P]),
+    "sdemc_price_f64": (_I, [_P, _P, ctypes.c_size_t, _P, _P]),
     "sdemc_price_noalloc_scratch_bytes": (ctypes.c_size_t, []),
     "sdemc_price_noalloc": (_I, [_P, _P, _P, _P, _P]),
     "sdemc_replay": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),

@@ -32,6 +32,21 @@ def price(inst, cfg=None, payoffs=None, device=None, out=None):
     return out
 
 
+def price_f64(inst, device=None, out=None):
+    """K11, the FP64 reference run on the same paths as :func:`price`.  Returns
+    a float64 CUDA tensor (sum, sum_sq, n, mean, var, status)."""
+    dev = _dev(device)
+    lib = N.load()
+    need = lib.sdemc_price_scratch_bytes(ctypes.byref(inst))
+    scratch = N.SCRATCH.get(need, dev)
+    if out is None:
+        out = torch.empty(6, dtype=torch.float64, device=dev)
+    rc = lib.sdemc_price_f64(ctypes.byref(inst), N.ptr(scratch), scratch.numel(), N.ptr(out),
+                             N.stream_handle(dev))
+    N.check(rc, "sdemc_price_f64")
+    return out
+
+
 def mlmc_level(inst, fine, coarse, h_fine, h_coarse, cfg=None, ys=None, device=None, out=None):
     """K2 launch for one level.  Returns float64 CUDA tensor
     (sumY, sumY2, n, sumPf, sumPf2, mean, var, status)."""
