@@ -560,7 +560,7 @@ def bench_accuracy(dev, line, served):
             rr = K.price_f64(q.phase(n_q, 1 << 44)).cpu().tolist()
             N.status_error(rr[5], "fp64 served reference")
             e = _err(x.mean, x.se, rr[3], math.sqrt(rr[4] / rr[2]))
-            e.update(target=q.target, dim=q.dim, fp64_paths=n_q, estimator=x.estimator_name(),
+            e.update(target=q.target, dim=q.dim, fp64_paths=n_q, estimator=x.estimator_name,
                      within_target=abs(e["err"]) <= q.target * abs(rr[3]))
             rows.append(e)
         out["served_sample"] = {
