@@ -160,8 +160,7 @@ def load_json_file(name):
     return None
 
 
-def fp32_peak_tflops(dev):
-    """Measured FFMA throughput of this GPU (best of 6 probe launches)."""
+def _probe(dev, name, iters):
     import ctypes
     import torch
     from sde_mc_gb300 import _native as N
@@ -173,11 +172,28 @@ def fp32_peak_tflops(dev):
     for _ in range(6):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        N.check(lib.sdemc_fp32_probe(4096, N.ptr(sink), 16, ctypes.byref(fl), s), "fp32 probe")
+        N.check(getattr(lib, name)(iters, N.ptr(sink), 16, ctypes.byref(fl), s), name)
         e1.record()
         torch.cuda.synchronize()
         best = max(best, fl.value / (e0.elapsed_time(e1) * 1e-3))
-    return best / 1e12
+    return best
+
+
+def fp32_peak_tflops(dev):
+    """Measured FFMA throughput of this GPU (best of 6 probe launches)."""
+    return _probe(dev, "sdemc_fp32_probe", 4096) / 1e12
+
+
+def mufu_peak_tops(dev):
+    """Measured special-function (MUFU) throughput, tera-ops/s."""
+    return _probe(dev, "sdemc_mufu_probe", 1024) / 1e12
+
+
+def mufu_per_path_step(d, jumps_per_step=0.0):
+    """M(d) = 2d + 1 MUFU operations per path-step (two per Box-Muller normal,
+    one for sqrt(dt)), plus 5 per jump event (log of the gap, a normal for the
+    mark, its exp)."""
+    return 2 * d + 1 + 5.0 * jumps_per_step
 
 
 def stream_windows(first, count):
@@ -256,7 +272,7 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------ sections ----
-def bench_rainbow_plain(dev, steps, warmup, fp32_peak):
+def bench_rainbow_plain(dev, steps, warmup, fp32_peak, mufu_peak):
     """The 2D rainbow at 1e-3 relative error with K1 (+K10), device-timed, L2
     flushed between steps; the FP32 roofline of price_kernel<2>."""
     import ctypes
@@ -317,6 +333,8 @@ def bench_rainbow_plain(dev, steps, warmup, fp32_peak):
             e2e.append(time.perf_counter() - t0)
     kernel_s = statistics.mean(k_ms) * 1e-3
     achieved = flops / kernel_s / 1e12
+    mufu_ops = n_target * steps_per_path * mufu_per_path_step(2, 2.0 / steps_per_path)
+    mufu_achieved = mufu_ops / kernel_s / 1e12
     traffic = (load_json_file(os.path.join("profiles", "kernel_traffic.json")) or {}).get("price_kernel<2,diag>")
     return {"workload": RAINBOW_WORKLOAD, "paths_per_price": n_target, "steps_per_path": steps_per_path,
             "prices_per_s": steps / (sum(k_ms) + sum(r_ms)) * 1e3, "ms_per_price": statistics.mean(
@@ -331,7 +349,11 @@ def bench_rainbow_plain(dev, steps, warmup, fp32_peak):
                                          "chunk partials only; paths stay in registers",
                          "kernel": "price_kernel<2,diag>", "kernel_ms": kernel_s * 1e3,
                          "flops_per_path_step": algorithmic_flops_per_path_step(2),
-                         "peak_source": "measured FFMA probe on this GPU (sdemc_fp32_probe)"},
+                         "peak_source": "measured FFMA probe on this GPU (sdemc_fp32_probe)",
+                         "mufu": {"achieved": mufu_achieved, "peak": mufu_peak, "unit": "Tops/s",
+                                  "frac": mufu_achieved / mufu_peak,
+                                  "ops_per_path_step": mufu_per_path_step(2, 2.0 / steps_per_path),
+                                  "peak_source": "measured rsqrt.approx probe (sdemc_mufu_probe)"}},
             "l2": "flushed (256 MB write) between timed steps", "gpu_launches": 2 * steps}
 
 
@@ -600,10 +622,12 @@ def bench_served(dev, steps, warmup, plain_windows, rank=0, world=1):
     srv.close()
     busy = st1["busy_s"] - st0["busy_s"]
     delta = {k: st1[k] - st0[k] for k in ("ticks", "launches", "h2d_bytes", "d2h_bytes", "path_steps")}
-    flops = 0.0
+    flops = mufu = 0.0
     for r in timed:
         x = res[r.idx]
         flops += (x.pilot_paths + x.main_paths) * r.path_steps * algorithmic_flops_per_path_step(r.dim)
+        jps = r.rate * float(r.inst.T) / r.path_steps
+        mufu += (x.pilot_paths + x.main_paths) * r.path_steps * mufu_per_path_step(r.dim, jps)
     # capacity: the same requests released at once (no arrival gaps)
     import copy
     burst = [copy.copy(r) for r in timed]
@@ -620,7 +644,8 @@ def bench_served(dev, steps, warmup, plain_windows, rank=0, world=1):
     S.run_plain(warm[:50])
     _, psumm = S.run_plain(plain_reqs)
     # price agreement between the two servers (each within its own error)
-    return {"summary": summ, "busy_s": busy, "delta": delta, "flops": flops, "plain": psumm, "capacity": capacity,
+    return {"summary": summ, "busy_s": busy, "delta": delta, "flops": flops, "mufu": mufu, "plain": psumm,
+            "capacity": capacity,
             "plain_windows": min(steps, plain_windows), "results": res, "timed": timed}
 
 
@@ -693,6 +718,7 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     dev = torch.device("cuda", local)
     fp32_peak = fp32_peak_tflops(dev)
+    mufu_peak = mufu_peak_tops(dev)
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
@@ -741,7 +767,11 @@ def main():
                                      "state and chunk partials only; paths stay in registers",
                      "kernel": "serve_kernel (all classes) over the server's device busy time",
                      "flops": "sum over requests of (pilot + main paths) x (steps + jump rate x T) x F(d)",
-                     "peak_source": "measured FFMA probe on this GPU (sdemc_fp32_probe)"},
+                     "peak_source": "measured FFMA probe on this GPU (sdemc_fp32_probe)",
+                     "mufu": {"achieved": b["mufu"] / busy / 1e12, "peak": mufu_peak, "unit": "Tops/s",
+                              "frac": b["mufu"] / busy / 1e12 / mufu_peak,
+                              "ops": "sum over requests of paths x (steps x (2d + 1) + 5 x jumps)",
+                              "peak_source": "measured rsqrt.approx probe (sdemc_mufu_probe)"}},
         "e2e": {"value": e2e, "unit": UNIT,
                 "h2d_bytes_per_step": b["delta"]["h2d_bytes"] / args.steps,
                 "d2h_bytes_per_step": b["delta"]["d2h_bytes"] / args.steps},
@@ -752,7 +782,7 @@ def main():
         line["clocks"] = clk.summary()
         secs = [s.strip() for s in args.sections.split(",") if s.strip() and s.strip() != "none"]
         if "rainbow" in secs:
-            line["rainbow2d_plain"] = _section(bench_rainbow_plain, dev, 20, 5, fp32_peak)
+            line["rainbow2d_plain"] = _section(bench_rainbow_plain, dev, 20, 5, fp32_peak, mufu_peak)
         if "mlmc" in secs:
             line["rainbow2d_mlmc"] = _section(bench_rainbow_mlmc, dev)
         if "mix" in secs:

@@ -184,6 +184,11 @@ int sdemc_device_sms(int* h_sms);
  * stream).  d_sink (sink_len floats) only keeps the chains live.           */
 int sdemc_fp32_probe(int iters, float* d_sink, int sink_len, double* h_flops,
                      void* stream);
+/* Special-function-unit (MUFU) throughput probe, same launch shape: 8
+ * independent rsqrt.approx chains per thread; *h_ops receives the MUFU
+ * operations of the launch.                                                */
+int sdemc_mufu_probe(int iters, float* d_sink, int sink_len, double* h_ops,
+                     void* stream);
 
 /* ---- K1: fused pricing ------------------------------------------------
  * Replaces mc_simple (sde_mc/mc.py:53-123) over JumpDiffusionSolver.solve
@@ -368,6 +373,20 @@ int sdemc_cv_backward(int dim, const float* d_params, const float* d_time,
 int sdemc_adam_step(float* d_params, const float* d_grad, float* d_m, float* d_v,
                     int nparam, int step, float lr, float beta1, float beta2,
                     float eps, void* stream);
+
+/* K6 on the 5th-generation tensor cores: the gradient of sdemc_cv_backward
+ * (same arguments and partial layout, d_mult as in sdemc_cv_forward_tc),
+ * every product a tcgen05.mma (forward recompute, the two dgrad products,
+ * the weight gradients accumulated in tensor memory over the CTA's rows).
+ * Uses at most nparts CTAs; a bounded wait that gives up sets SDEMC_ETIMEOUT
+ * in *d_status and NaN in the gradient.  Replaces loss.backward() inside
+ * train_adapted_control_variates (sde_mc/varred.py:160-180).               */
+int sdemc_cv_backward_tc(int dim, const float* d_params, const float* d_time,
+                         const float* d_paths, const float* d_mult,
+                         const int64_t* d_index, int64_t n, int steps,
+                         float disc_rate, const float* d_gamma,
+                         float* d_partials, int nparts, float* d_grad,
+                         int32_t* d_status, void* stream);
 
 /* K5 on the 5th-generation tensor cores (tcgen05.mma, accumulators in tensor
  * memory) for large batches: d_gamma[q] = payoff[index[q]] + sum_k

@@ -86,6 +86,8 @@ _PROTOS = {
     "sdemc_cv_backward": (_I, [_I, _P, _P, _P, _P, _P, ctypes.c_int64, _I, ctypes.c_float, _P, _P, _I, _P, _P]),
     "sdemc_adam_step": (_I, [_P, _P, _P, _P, _I, _I, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                              ctypes.c_float, _P]),
+    "sdemc_cv_backward_tc": (_I, [_I, _P, _P, _P, _P, _P, ctypes.c_int64, _I, ctypes.c_float, _P, _P, _I, _P, _P,
+                                  _P]),
     "sdemc_cv_forward_tc_scratch_bytes": (ctypes.c_size_t, [ctypes.c_int64, _I]),
     "sdemc_cv_forward_tc": (_I, [_I, _P, _P, _P, _P, _P, _P, ctypes.c_int64, _I, ctypes.c_float, _P, _P,
                                  ctypes.c_size_t, _P, _P]),
@@ -111,6 +113,7 @@ _PROTOS = {
     "sdemc_philox": (_I, [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64,
                           ctypes.c_uint32, _I, _P, _P]),
     "sdemc_fp32_probe": (_I, [_I, _P, _I, ctypes.POINTER(ctypes.c_double), _P]),
+    "sdemc_mufu_probe": (_I, [_I, _P, _I, ctypes.POINTER(ctypes.c_double), _P]),
 }
 EXPORTED = tuple(_PROTOS)
 

@@ -168,9 +168,37 @@ __global__ void __launch_bounds__(256) fp32_probe_kernel(int iters, float b, flo
   if (s == never) out[blockIdx.x % out_len] = s;
 }
 
+// MUFU throughput probe: 8 independent reciprocal-square-root chains per
+// thread (rsqrt.approx is one special-function-unit operation; the chains
+// converge to 1 and stay finite), full occupancy.
+__global__ void __launch_bounds__(256) mufu_probe_kernel(int iters, float never, float* out, int out_len) {
+  float a[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) a[j] = 1.5f + (threadIdx.x + j) * 1e-3f;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) asm("rsqrt.approx.ftz.f32 %0, %0;" : "+f"(a[j]));
+    }
+  }
+  const float s = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
+  if (s == never) out[blockIdx.x % out_len] = s;
+}
+
 }  // namespace sdemc
 
 using namespace sdemc;
+
+extern "C" int sdemc_mufu_probe(int iters, float* d_sink, int sink_len, double* h_ops, void* stream) {
+  if (iters < 1 || !h_ops || !d_sink || sink_len < 1) return fail(SDEMC_EINVAL, "bad probe args");
+  const int sms = num_sms();
+  if (sms <= 0) return fail(SDEMC_ECUDA, "no CUDA device");
+  const int blocks = sms * 8;
+  mufu_probe_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(iters, __builtin_nanf(""), d_sink, sink_len);
+  *h_ops = (double)blocks * 256.0 * iters * 32.0;
+  return check_cuda(cudaGetLastError(), "mufu_probe_kernel launch");
+}
 
 extern "C" int sdemc_fp32_probe(int iters, float* d_sink, int sink_len, double* h_flops, void* stream) {
   if (iters < 1 || !h_flops || !d_sink || sink_len < 1) return fail(SDEMC_EINVAL, "bad probe args");

@@ -55,20 +55,36 @@ SDEMC_DI uint64_t smem_desc(uint32_t saddr, uint32_t sbo) {
          (1ull << 46);
 }
 
+// The same with an explicit leading-dimension byte offset.  K-major: LBO =
+// distance of K-adjacent core matrices, SBO = of 8-row groups.  MN-major (8
+// MN-contiguous elements x 8 K rows per core matrix): LBO = distance of 8-row
+// K groups, SBO = of MN-adjacent core matrices.
+SDEMC_DI uint64_t smem_desc_lbo(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+         (1ull << 46);
+}
+
+// kind::f16 instruction descriptor for M x N, BF16 operands, FP32 accumulator;
+// a_mn / b_mn select MN-major operands (bits 15, 16).
+constexpr uint32_t make_idesc(int M, int N, bool a_mn, bool b_mn) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((a_mn ? 1u : 0u) << 15) | ((b_mn ? 1u : 0u) << 16) |
+         ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
 SDEMC_DI uint32_t saddr_of(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 SDEMC_DI void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 SDEMC_DI void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 SDEMC_DI void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-SDEMC_DI void tmem_alloc(uint32_t slot_saddr) {  // whole warp
+SDEMC_DI void tmem_alloc(uint32_t slot_saddr, uint32_t ncols = kTmemCols) {  // whole warp
   asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot_saddr),
-               "r"((uint32_t)kTmemCols)
+               "r"(ncols)
                : "memory");
   asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
 }
-SDEMC_DI void tmem_dealloc(uint32_t taddr) {  // whole warp
-  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"((uint32_t)kTmemCols)
+SDEMC_DI void tmem_dealloc(uint32_t taddr, uint32_t ncols = kTmemCols) {  // whole warp
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
                : "memory");
 }
 
@@ -96,6 +112,13 @@ SDEMC_DI void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t 
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
       "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+      : "memory");
+}
+SDEMC_DI void mma_f16_id(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
       : "memory");
 }
 SDEMC_DI void mma_commit(uint32_t mbar_saddr) {
@@ -156,12 +179,13 @@ SDEMC_DI void put_bf16(unsigned char* M, int r, int k, int K, __nv_bfloat16 v) {
   *reinterpret_cast<__nv_bfloat16*>(M + core_offset(r, k, K)) = v;
 }
 
-// CTA-wide setup: operands into shared memory, mbarrier, tensor memory.
+// The weight operands of layers 1-3 (BF16, K-major): B1 (64 x 16: W1 and b1
+// split into high and low parts), B2, B3 (64 x 80: W | b high | b low | 0).
 template <int D>
-SDEMC_DI void setup(TcSmem& sm, const float* prm) {
+SDEMC_DI void fill_weights(unsigned char* B1, unsigned char* B2, unsigned char* B3, const float* prm) {
   using L = TcLayout<D>;
   const int t = threadIdx.x;
-  const __nv_bfloat16 one = __float2bfloat16_rn(1.f), zero = __float2bfloat16_rn(0.f);
+  const __nv_bfloat16 zero = __float2bfloat16_rn(0.f);
   for (int e = t; e < kH * kKH; e += blockDim.x) {
     const int n = e / kKH, k = e % kKH;
     __nv_bfloat16 v2 = zero, v3 = zero;
@@ -175,8 +199,8 @@ SDEMC_DI void setup(TcSmem& sm, const float* prm) {
       split(prm[L::B3 + n], h, l);
       v3 = k == kH ? h : l;
     }
-    put_bf16(sm.B2, n, k, kKH, v2);
-    put_bf16(sm.B3, n, k, kKH, v3);
+    put_bf16(B2, n, k, kKH, v2);
+    put_bf16(B3, n, k, kKH, v3);
   }
   // layer 1: columns 3i, 3i+1, 3i+2 of input i = (xh, xl, xh) against
   // (wh, wh, wl); columns 3(D+1), +1 = ones against (bh, bl)
@@ -192,8 +216,17 @@ SDEMC_DI void setup(TcSmem& sm, const float* prm) {
       split(prm[L::B1 + n], h, l);
       v = k == 3 * (D + 1) ? h : l;
     }
-    put_bf16(sm.B1, n, k, kK1, v);
+    put_bf16(B1, n, k, kK1, v);
   }
+}
+
+// CTA-wide setup: operands into shared memory, mbarrier, tensor memory.
+template <int D>
+SDEMC_DI void setup(TcSmem& sm, const float* prm) {
+  using L = TcLayout<D>;
+  const int t = threadIdx.x;
+  const __nv_bfloat16 one = __float2bfloat16_rn(1.f), zero = __float2bfloat16_rn(0.f);
+  fill_weights<D>(sm.B1, sm.B2, sm.B3, prm);
   // the A tile's bias and padding columns never change: ones, then zeros
   for (int e = t; e < kRows * (kKH - kH); e += blockDim.x) {
     const int r = e / (kKH - kH), k = kH + e % (kKH - kH);
@@ -280,7 +313,7 @@ SDEMC_DI void relu_layer4(TcSmem& sm, float* out) {
 
 // Layer 1's A row: (th, tl, th, x0h, x0l, x0h, ..., 1, 1, 0 ...).
 template <int D>
-SDEMC_DI void inputs_to_A1(TcSmem& sm, float t, const float* x) {
+SDEMC_DI void inputs_to_tile(unsigned char* A1, float t, const float* x) {
   __nv_bfloat16 a[kK1];
   const __nv_bfloat16 one = __float2bfloat16_rn(1.f), zero = __float2bfloat16_rn(0.f);
 #pragma unroll
@@ -302,9 +335,11 @@ SDEMC_DI void inputs_to_A1(TcSmem& sm, float t, const float* x) {
     q.y = pack2b(a[8 * c + 2], a[8 * c + 3]);
     q.z = pack2b(a[8 * c + 4], a[8 * c + 5]);
     q.w = pack2b(a[8 * c + 6], a[8 * c + 7]);
-    *reinterpret_cast<uint4*>(sm.A1 + core_offset(threadIdx.x, 8 * c, kK1)) = q;
+    *reinterpret_cast<uint4*>(A1 + core_offset(threadIdx.x, 8 * c, kK1)) = q;
   }
 }
+template <int D>
+SDEMC_DI void inputs_to_A1(TcSmem& sm, float t, const float* x) { inputs_to_tile<D>(sm.A1, t, x); }
 
 // The network on the CTA's 128 rows (this thread: row threadIdx.x with
 // inputs t, x); out[D] = f(t, x).  All 128 threads call it together, the same

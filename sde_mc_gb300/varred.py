@@ -181,6 +181,19 @@ class GpuCv:
         N.check(rc, "sdemc_cv_backward")
         return self.grad
 
+    def backward_tc(self, data, rate, gamma, idx=None):
+        """K6 on tcgen05: the same gradient, every product on the 5th-generation
+        tensor cores (the weight gradients accumulated in tensor memory)."""
+        n = data.n if idx is None else int(idx.numel())
+        if self._tc_status is None:
+            self._tc_status = torch.zeros(1, dtype=torch.int32, device=self.device)
+        rc = N.load().sdemc_cv_backward_tc(self.dim, N.ptr(self.params), N.ptr(data.time), N.ptr(data.paths),
+                                           N.ptr(data.normals), N.ptr(idx), n, data.steps, float(rate),
+                                           N.ptr(gamma), N.ptr(self.partials), self.nparts, N.ptr(self.grad),
+                                           N.ptr(self._tc_status), N.stream_handle(self.device))
+        N.check(rc, "sdemc_cv_backward_tc")
+        return self.grad
+
     def adam(self, lr=1e-3, betas=(0.9, 0.999), eps=1e-8):
         self.step_count += 1
         rc = N.load().sdemc_adam_step(N.ptr(self.params), N.ptr(self.grad), N.ptr(self.m), N.ptr(self.v),
@@ -222,6 +235,10 @@ def adam_hparams(opt):
     return float(lr if not torch.is_tensor(lr) else lr.item()), tuple(grp["betas"]), float(grp["eps"])
 
 
+# K6 on tcgen05 for the training gradient (False: the mma.sync kernel)
+BACKWARD_TC = True
+
+
 def train_gpu(cvs, datas, rate, epochs, batch_size, lr, betas, eps, print_losses=False, early_stopping=None,
               generator=None):
     """Minibatch training of the networks ``cvs`` (one data set each, same
@@ -245,10 +262,16 @@ def train_gpu(cvs, datas, rate, epochs, batch_size, lr, betas, eps, print_losses
                 gamma += cv.forward(data, rate, idx)
             losses[b] = gamma.double().var()
             for cv, data in zip(cvs, datas):
-                cv.backward(data, rate, gamma, idx)
+                if BACKWARD_TC:
+                    cv.backward_tc(data, rate, gamma, idx)
+                else:
+                    cv.backward(data, rate, gamma, idx)
             for cv in cvs:
                 cv.adam(lr, betas, eps)
         loss_arr.append(float(losses.mean()))
+        if BACKWARD_TC:
+            for cv in cvs:
+                N.status_error(int(cv._tc_status.item()), "control-variate gradient (tensor cores)")
         if print_losses:
             print('{}: Train loss: {:.5f}     95% confidence interval: {:.5f}'.format(
                 epoch, loss_arr[-1], np.sqrt(loss_arr[-1]) * 2 / np.sqrt(n)))

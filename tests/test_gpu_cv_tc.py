@@ -1,6 +1,6 @@
-"""K5 on tcgen05 (tensor-memory accumulators) against the mma.sync kernel and
-the oracle's precision-policy restatement: both round the same BF16
-operands, so Gamma agrees to accumulation-order noise."""
+"""K5 and K6 on tcgen05 (tensor-memory accumulators) against the mma.sync
+kernels and the oracle's precision-policy restatement: both round the same
+BF16 operands, so Gamma and the gradients agree to accumulation-order noise."""
 import numpy as np
 import pytest
 import torch
@@ -42,3 +42,52 @@ def test_tc_forward_large_batch_and_index(d):
     idx = torch.randperm(data.n, device=DEV)[:777]
     g_idx = cv.forward_tc(data, 0.02, idx=idx)
     torch.testing.assert_close(g_idx, g_tc[idx], rtol=0, atol=0)
+
+
+def _layer_norms(g, ref_layers):
+    off, out = 0, []
+    for m in ref_layers:
+        m = np.asarray(m).reshape(-1)
+        out.append((np.linalg.norm(g[off:off + m.size] - m), np.linalg.norm(m)))
+        off += m.size
+    assert off == g.size
+    return out
+
+
+def test_tc_backward_matches_oracle_and_mma(oracle_mod):
+    fx, data, params = _fixture()
+    n, S, d = fx["normals"].shape
+    cv = V.GpuCv(_net(d, params), d, DEV)
+    gamma = torch.from_numpy(fx["gamma"]).to(DEV)
+    g_tc = cv.backward_tc(data, float(fx["r"]), gamma).cpu().numpy().copy()
+    assert int(cv._tc_status.item()) == 0
+    g_mma = cv.backward(data, float(fx["r"]), gamma).cpu().numpy().copy()
+    mixed = oracle_mod.cv_grads_mixed(params, fx["time"][..., 0], fx["paths"], fx["normals"], fx["gamma"],
+                                      float(fx["r"]))
+    for i, (e, m) in enumerate(_layer_norms(g_tc, mixed)):
+        assert e <= 5e-3 * m + 1e-9, ("oracle", i, e / m)
+    sizes = [np.asarray(m).size for m in mixed]
+    split = np.split(g_mma, np.cumsum(sizes)[:-1])
+    for i, (e, m) in enumerate(_layer_norms(g_tc, split)):
+        assert e <= 5e-3 * m + 1e-9, ("mma.sync", i, e / m)
+    g2 = cv.backward_tc(data, float(fx["r"]), gamma).cpu().numpy()
+    np.testing.assert_array_equal(g_tc, g2)
+
+
+@pytest.mark.parametrize("d", [1, 2])
+def test_tc_backward_large_batch_and_index(d):
+    solver, payoff, disc = (merton1d(40, seed=6) if d == 1 else indep2d(40, seed=6))
+    dl = sm.simulate_adapted_data(20000, solver, payoff, disc, bs=20000, inference=True)
+    data = V.CvData.from_dataset(dl.dataset, solver, DEV)
+    cv = V.GpuCv(_net(d, seed=11), d, DEV)
+    idx = torch.randperm(data.n, device=DEV)[:4096]
+    gamma = cv.forward(data, 0.02, idx)
+    g_tc = cv.backward_tc(data, 0.02, gamma, idx).cpu().numpy().copy()
+    assert int(cv._tc_status.item()) == 0
+    g_mma = cv.backward(data, 0.02, gamma, idx).cpu().numpy().copy()
+    # parameter layout: W1, b1, W2, b2, W3, b3, W4, b4
+    IN, H = d + 1, 64
+    sizes = [H * IN, H, H * H, H, H * H, H, d * H, d]
+    parts = np.split(g_mma, np.cumsum(sizes)[:-1])
+    for i, (e, m) in enumerate(_layer_norms(g_tc, parts)):
+        assert e <= 5e-3 * m + 1e-9, (i, e / m)
