@@ -141,6 +141,8 @@ class GpuCv:
         self.grad = torch.zeros_like(self.params)
         self.nparts = 2 * _sms()
         self.partials = torch.empty((self.nparts, self.nparam), dtype=torch.float32, device=device)
+        self._tc_status = None
+        self._bwd_status = torch.zeros(1, dtype=torch.int32, device=device)
 
     def forward(self, data, rate, idx=None, gamma=None, fout=None):
         n = data.n if idx is None else int(idx.numel())
@@ -185,12 +187,10 @@ class GpuCv:
         """K6 on tcgen05: the same gradient, every product on the 5th-generation
         tensor cores (the weight gradients accumulated in tensor memory)."""
         n = data.n if idx is None else int(idx.numel())
-        if self._tc_status is None:
-            self._tc_status = torch.zeros(1, dtype=torch.int32, device=self.device)
         rc = N.load().sdemc_cv_backward_tc(self.dim, N.ptr(self.params), N.ptr(data.time), N.ptr(data.paths),
                                            N.ptr(data.normals), N.ptr(idx), n, data.steps, float(rate),
                                            N.ptr(gamma), N.ptr(self.partials), self.nparts, N.ptr(self.grad),
-                                           N.ptr(self._tc_status), N.stream_handle(self.device))
+                                           N.ptr(self._bwd_status), N.stream_handle(self.device))
         N.check(rc, "sdemc_cv_backward_tc")
         return self.grad
 
@@ -271,7 +271,7 @@ def train_gpu(cvs, datas, rate, epochs, batch_size, lr, betas, eps, print_losses
         loss_arr.append(float(losses.mean()))
         if BACKWARD_TC:
             for cv in cvs:
-                N.status_error(int(cv._tc_status.item()), "control-variate gradient (tensor cores)")
+                N.status_error(int(cv._bwd_status.item()), "control-variate gradient (tensor cores)")
         if print_losses:
             print('{}: Train loss: {:.5f}     95% confidence interval: {:.5f}'.format(
                 epoch, loss_arr[-1], np.sqrt(loss_arr[-1]) * 2 / np.sqrt(n)))

@@ -60,7 +60,7 @@ def test_tc_backward_matches_oracle_and_mma(oracle_mod):
     cv = V.GpuCv(_net(d, params), d, DEV)
     gamma = torch.from_numpy(fx["gamma"]).to(DEV)
     g_tc = cv.backward_tc(data, float(fx["r"]), gamma).cpu().numpy().copy()
-    assert int(cv._tc_status.item()) == 0
+    assert int(cv._bwd_status.item()) == 0
     g_mma = cv.backward(data, float(fx["r"]), gamma).cpu().numpy().copy()
     mixed = oracle_mod.cv_grads_mixed(params, fx["time"][..., 0], fx["paths"], fx["normals"], fx["gamma"],
                                       float(fx["r"]))
@@ -83,7 +83,7 @@ def test_tc_backward_large_batch_and_index(d):
     idx = torch.randperm(data.n, device=DEV)[:4096]
     gamma = cv.forward(data, 0.02, idx)
     g_tc = cv.backward_tc(data, 0.02, gamma, idx).cpu().numpy().copy()
-    assert int(cv._tc_status.item()) == 0
+    assert int(cv._bwd_status.item()) == 0
     g_mma = cv.backward(data, 0.02, gamma, idx).cpu().numpy().copy()
     # parameter layout: W1, b1, W2, b2, W3, b3, W4, b4
     IN, H = d + 1, 64
