@@ -677,9 +677,14 @@ def profile_cv(n):
     data = V.CvData.from_dataset(dl.dataset, solver, dev)
     for i in range(3):
         g = cv.forward_tc(data, 0.02)
+    idx = torch.arange(min(4096, data.n), device=dev)
+    gb = cv.forward(data, 0.02, idx)
+    for i in range(3):
+        cv.backward_tc(data, 0.02, gb, idx)
     torch.cuda.synchronize()
     print(json.dumps({"profile_cv": n, "k7": r.cpu().tolist(), "tc_status": int(cv._tc_status.item()),
-                      "tc_mean": float(g.double().mean())}))
+                      "tc_mean": float(g.double().mean()), "bwd_status": int(cv._bwd_status.item()),
+                      "grad_norm": float(cv.grad.norm())}))
 
 
 def profile_launches(n):
