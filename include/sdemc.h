@@ -156,7 +156,7 @@ enum {
 typedef struct sdemc_cfg {
   int32_t block_threads;   /* threads per CTA (multiple of 32), 0 = auto    */
   int32_t ctas_per_sm;     /* persistent grid = SMs x this, 0 = auto        */
-  int32_t interleave;      /* path rounds a lane runs together: 1, 2 or 4   */
+  int32_t interleave;      /* paths a lane steps together: 1 or 2 (0 = 1)   */
   int32_t flags;           /* SDEMC_CFG_*                                   */
   int64_t timeout_ns;      /* bound for device-side waits, 0 = default      */
 } sdemc_cfg;

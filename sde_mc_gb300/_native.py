@@ -30,6 +30,7 @@ MODEL_AFFINE, MODEL_HESTON, MODEL_ASIAN = 0, 1, 2
 (PAYOFF_EUROCALL, PAYOFF_EUROPUT, PAYOFF_BINARY_AON, PAYOFF_BASKET_ARITH, PAYOFF_BASKET_GEO,
  PAYOFF_RAINBOW, PAYOFF_DIGITAL, PAYOFF_BESTOF, PAYOFF_ASIANCALL, PAYOFF_HESTON_RAINBOW) = range(10)
 CFG_EXACT_EULER = 1
+INST_PAYOFF_AT_NOMINAL_STEP = 1
 
 _f8 = ctypes.c_float * MAX_DIM
 

@@ -59,7 +59,8 @@ int validate_inst(const sdemc_inst* I) {
   if (I->model > SDEMC_MODEL_ASIAN) return fail(SDEMC_EINVAL, "model %u unknown", I->model);
   if (I->model != SDEMC_MODEL_AFFINE && (I->dim != 2 || I->noise != SDEMC_NOISE_DIAG))
     return fail(SDEMC_EUNSUPPORTED, "Heston and Asian models are 2-D with 'diag' noise");
-  if (I->model == SDEMC_MODEL_HESTON && I->rate > 0.f) return fail(SDEMC_EUNSUPPORTED, "Heston has no jumps");
+  if (I->model == SDEMC_MODEL_HESTON && (I->rate > 0.f || I->grid != SDEMC_GRID_UNIFORM))
+    return fail(SDEMC_EUNSUPPORTED, "Heston runs on the uniform grid (HestonSolver), without jumps");
   if (I->model == SDEMC_MODEL_ASIAN && I->jump_target != SDEMC_JUMP_COMMON)
     return fail(SDEMC_EUNSUPPORTED, "the Asian integral takes common jumps only");
   return SDEMC_OK;

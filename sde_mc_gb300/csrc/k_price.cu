@@ -20,7 +20,29 @@ struct PriceParams {
   RoundKeys rk;
 };
 
-template <int D, int NOISE, int MODE>
+// Payoff of lane path p (terminal state x) and the chunk's FP32 butterfly
+// sums, stored as chunk c's FP64 partial.
+template <int D>
+SDEMC_DI void emit_chunk(const sdemc_inst& I, const float* x, int64_t p, int64_t c, double* part,
+                         float* payoffs) {
+  const int lane = threadIdx.x & 31;
+  const bool valid = p < I.num_paths;
+  const float pay = __fmul_rn(payoff<D>(I, x), I.discount);
+  const float v = valid ? pay : 0.f;
+  if (valid && payoffs) payoffs[p] = pay;
+  const float s = warp_sum(v);
+  const float s2 = warp_sum(__fmul_rn(v, v));
+  const int n = __popc(__ballot_sync(kFull, valid));
+  if (lane == 0) {
+    part[c * 3 + 0] = (double)s;
+    part[c * 3 + 1] = (double)s2;
+    part[c * 3 + 2] = (double)n;
+  }
+}
+
+// PATHS = paths per lane: 1, or 2 (chunks c and c + 1 stepped together by
+// simulate2; the same bits per chunk).
+template <int D, int NOISE, int MODE, int PATHS>
 __global__ void __launch_bounds__(256)
 price_kernel(const __grid_constant__ PriceParams P, double* __restrict__ part,
              float* __restrict__ payoffs, int32_t* __restrict__ status, int64_t nchunks,
@@ -30,24 +52,26 @@ price_kernel(const __grid_constant__ PriceParams P, double* __restrict__ part,
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   bool ovf = false;
-  for (int64_t c = warp; c < nchunks; c += nwarps) {
+  for (int64_t c = warp * PATHS; c < nchunks; c += nwarps * PATHS) {
     const int64_t p = c * kChunk + lane;
-    NativeDraws<D, NOISE> dr;
-    dr.init(I, (uint64_t)p, ConstKeys{&P.rk});
-    NullSink sk;
-    float x[D];
-    simulate<D, NOISE, MODE>(I, dr, sk, x, max_iters, ovf);
-    const bool valid = p < I.num_paths;
-    const float pay = __fmul_rn(payoff<D>(I, x), I.discount);
-    const float v = valid ? pay : 0.f;
-    if (valid && payoffs) payoffs[p] = pay;
-    const float s = warp_sum(v);
-    const float s2 = warp_sum(__fmul_rn(v, v));
-    const int n = __popc(__ballot_sync(kFull, valid));
-    if (lane == 0) {
-      part[c * 3 + 0] = (double)s;
-      part[c * 3 + 1] = (double)s2;
-      part[c * 3 + 2] = (double)n;
+    if (PATHS == 1) {
+      NativeDraws<D, NOISE> dr;
+      dr.init(I, (uint64_t)p, ConstKeys{&P.rk});
+      NullSink sk;
+      float x[D];
+      simulate<D, NOISE, MODE>(I, dr, sk, x, max_iters, ovf);
+      emit_chunk<D>(I, x, p, c, part, payoffs);
+    } else {
+      // the partner chunk c + 1 may lie past the end: its paths run (beyond
+      // num_paths, like the tail lanes of a last chunk) and are not stored
+      const int64_t pb = p + kChunk;
+      NativeDraws<D, NOISE> da, db;
+      da.init(I, (uint64_t)p, ConstKeys{&P.rk});
+      db.init(I, (uint64_t)pb, ConstKeys{&P.rk});
+      float xa[D], xb[D];
+      simulate2<D, NOISE, MODE>(I, da, db, xa, xb, max_iters, ovf);
+      emit_chunk<D>(I, xa, p, c, part, payoffs);
+      if (c + 1 < nchunks) emit_chunk<D>(I, xb, pb, c + 1, part, payoffs);
     }
   }
   if (ovf) atomicOr(status, SDEMC_EOVERFLOW);
@@ -56,7 +80,8 @@ price_kernel(const __grid_constant__ PriceParams P, double* __restrict__ part,
 template <int D, int NOISE, int MODE>
 static int launch_price_t(const sdemc_inst& I, const sdemc_cfg& cfg, double* part,
                           float* payoffs, int32_t* status, int64_t nchunks, cudaStream_t s) {
-  auto kern = price_kernel<D, NOISE, MODE>;
+  const int paths = cfg.interleave == 2 ? 2 : 1;
+  auto kern = paths == 2 ? price_kernel<D, NOISE, MODE, 2> : price_kernel<D, NOISE, MODE, 1>;
   const int threads = cfg.block_threads > 0 ? cfg.block_threads : 128;
   int per_sm = 0;
   int rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0),
@@ -65,8 +90,8 @@ static int launch_price_t(const sdemc_inst& I, const sdemc_cfg& cfg, double* par
   if (cfg.ctas_per_sm > 0 && cfg.ctas_per_sm < per_sm) per_sm = cfg.ctas_per_sm;
   if (per_sm < 1) per_sm = 1;
   const int64_t resident = (int64_t)num_sms() * per_sm;
-  const int64_t warps_per_cta = threads / 32;
-  int64_t ctas = (nchunks + warps_per_cta - 1) / warps_per_cta;
+  const int64_t chunks_per_cta = threads / 32 * paths;
+  int64_t ctas = (nchunks + chunks_per_cta - 1) / chunks_per_cta;
   if (ctas > resident) ctas = resident;
   if (ctas < 1) ctas = 1;
   PriceParams P;
@@ -95,6 +120,8 @@ extern "C" int sdemc_price_chunks(const sdemc_inst* h_inst, const sdemc_cfg* h_c
                 sdemc_price_scratch_bytes(h_inst));
   if (h_cfg && (h_cfg->block_threads % 32 != 0 || h_cfg->block_threads > 256 || h_cfg->block_threads < 0))
     return fail(SDEMC_EINVAL, "block_threads %d: need a multiple of 32 in [32, 256]", h_cfg->block_threads);
+  if (h_cfg && (h_cfg->interleave < 0 || h_cfg->interleave > 2))
+    return fail(SDEMC_EINVAL, "interleave %d: paths per lane are 1 or 2 (0 = 1)", h_cfg->interleave);
   sdemc_cfg cfg{};
   if (h_cfg) cfg = *h_cfg;
   const sdemc_inst& I = *h_inst;

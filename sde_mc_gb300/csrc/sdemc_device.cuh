@@ -677,6 +677,104 @@ SDEMC_DI int simulate(const sdemc_inst& I, Draws& dr, Sink& sk, float* x, int ma
   return own;
 }
 
+// Two paths per lane (paths-per-thread tiling): simulate() with a NullSink for
+// paths a and b stepped together.  Each path goes through exactly the
+// operations simulate() gives it (a path that has reached T takes dt = 0
+// steps, which leave it unchanged, while its partner still runs; the jump
+// stream of a path is its blocks 0, 1, 2, ... whoever draws them), so both
+// end bit-identical to simulate()'s; the two instruction streams are
+// independent and give the scheduler twice the work between waits.
+template <int D, int NOISE, int MODE, class Draws>
+SDEMC_DI void simulate2(const sdemc_inst& I, Draws& da, Draws& db, float* xa, float* xb, int max_iters,
+                        bool& overflow) {
+  using L = Layout<D, NOISE>;
+  constexpr bool EXACT = (MODE & kModeExact) != 0;
+  float dWa[D], dW2a[D], za[L::ZD], dWb[D], dW2b[D], zb[L::ZD];
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    xa[i] = I.x0[i]; xb[i] = I.x0[i];
+    dW2a[i] = 0.f; dW2b[i] = 0.f;
+  }
+  if (I.grid == SDEMC_GRID_UNIFORM) {
+    const float h = I.h;
+    for (int k = 0; k < I.num_steps; ++k) {
+      da.increments(I, k, h, dWa, dW2a, za);
+      db.increments(I, k, h, dWb, dW2b, zb);
+      euler<D, NOISE, EXACT>(I, xa, h, dWa, dW2a);
+      euler<D, NOISE, EXACT>(I, xb, h, dWb, dW2b);
+    }
+    return;
+  }
+  const float T = I.T;
+  float ha = I.h, hb = I.h, ta = 0.f, tb = 0.f;
+  float nja = da.jump_first(I), njb = db.jump_first(I);
+  int owna = 0, ownb = 0, k = 0;
+  bool acta = ta < T, actb = tb < T;
+  constexpr int NC = (MODE & kModeNominal) ? D : 1;
+  float capa[NC], capb[NC];
+  if (MODE & kModeNominal) {
+#pragma unroll
+    for (int i = 0; i < D; ++i) { capa[i] = xa[i]; capb[i] = xb[i]; }
+  }
+  while (__any_sync(kFull, acta || actb)) {
+    if (k >= max_iters) { overflow = true; break; }
+    ha = fminf(ha, fmaxf(__fsub_rn(T, ta), 0.f));
+    hb = fminf(hb, fmaxf(__fsub_rn(T, tb), 0.f));
+    float dta = fminf(ha, __fsub_rn(nja, ta));
+    float dtb = fminf(hb, __fsub_rn(njb, tb));
+    if (!acta) dta = 0.f;
+    if (!actb) dtb = 0.f;
+    da.increments(I, k, dta, dWa, dW2a, za);
+    db.increments(I, k, dtb, dWb, dW2b, zb);
+    float olda[D], oldb[D];
+#pragma unroll
+    for (int i = 0; i < D; ++i) { olda[i] = xa[i]; oldb[i] = xb[i]; }
+    euler<D, NOISE, EXACT>(I, xa, dta, dWa, dW2a);
+    euler<D, NOISE, EXACT>(I, xb, dtb, dWb, dW2b);
+    ta = __fadd_rn(ta, dta);
+    tb = __fadd_rn(tb, dtb);
+    if (acta && jump_due(nja, ta)) {
+      float J;
+      int sel;
+      nja = da.on_fire(I, k, nja, J, sel);
+      apply_jump<D, EXACT>(I, xa, I.exact_jumps ? xa : olda, J, sel);
+    }
+    if (actb && jump_due(njb, tb)) {
+      float J;
+      int sel;
+      njb = db.on_fire(I, k, njb, J, sel);
+      apply_jump<D, EXACT>(I, xb, I.exact_jumps ? xb : oldb, J, sel);
+    }
+    owna += acta ? 1 : 0;
+    ownb += actb ? 1 : 0;
+    if (MODE & kModeNominal) {
+      if (acta && owna == I.num_steps) {
+#pragma unroll
+        for (int i = 0; i < D; ++i) capa[i] = xa[i];
+      }
+      if (actb && ownb == I.num_steps) {
+#pragma unroll
+        for (int i = 0; i < D; ++i) capb[i] = xb[i];
+      }
+    }
+    ++k;
+    acta = ta < T;
+    actb = tb < T;
+    da.after_step(I, k, nja, acta);
+    db.after_step(I, k, njb, actb);
+  }
+  if (MODE & kModeNominal) {
+    if (owna >= I.num_steps) {
+#pragma unroll
+      for (int i = 0; i < D; ++i) xa[i] = capa[i];
+    }
+    if (ownb >= I.num_steps) {
+#pragma unroll
+      for (int i = 0; i < D; ++i) xb[i] = capb[i];
+    }
+  }
+}
+
 // Warp sum (fixed xor butterfly: every lane ends with the same bits).
 SDEMC_DI float warp_sum(float v) {
 #pragma unroll

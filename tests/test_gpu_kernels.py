@@ -182,9 +182,31 @@ def test_fused_price_matches_materialised_and_reduction(name, oracle_mod):
 def test_price_invariant_to_launch_shape():
     inst = inst_for(indep2d(64), num_paths=100_000, seed=3)
     base = np_(K.price(inst))
-    for bt, cps in [(32, 1), (64, 3), (256, 2), (128, 0), (96, 5)]:
-        cfg = N.SdemcCfg(block_threads=bt, ctas_per_sm=cps)
+    for bt, cps, il in [(32, 1, 1), (64, 3, 1), (256, 2, 1), (128, 0, 0), (96, 5, 1), (128, 0, 2), (64, 3, 2),
+                        (256, 1, 2)]:
+        cfg = N.SdemcCfg(block_threads=bt, ctas_per_sm=cps, interleave=il)
         np.testing.assert_array_equal(np_(K.price(inst, cfg=cfg)), base)
+
+
+@pytest.mark.parametrize("name", ["merton1d", "merton2d_exact", "indep2d", "gbm_uniform", "basket5", "double_gbm",
+                                  "heston", "asian_merton"])
+def test_two_paths_per_lane_is_bit_identical(name):
+    """Paths-per-thread tiling (cfg.interleave = 2, simulate2) gives every path
+    the bits of the one-path loop: payoffs and sums, odd chunk counts included."""
+    case = EXPORT_CASES[name]()
+    for n in (32 * 7 + 5, 20000):
+        inst = inst_for(case, num_paths=n, seed=13, path_offset=77)
+        p1 = torch.empty(n, dtype=torch.float32, device="cuda")
+        p2 = torch.empty(n, dtype=torch.float32, device="cuda")
+        r1 = np_(K.price(inst, payoffs=p1))
+        r2 = np_(K.price(inst, cfg=N.SdemcCfg(interleave=2), payoffs=p2))
+        np.testing.assert_array_equal(np_(p1), np_(p2))
+        np.testing.assert_array_equal(r1, r2)
+    inst.flags |= N.INST_PAYOFF_AT_NOMINAL_STEP
+    np.testing.assert_array_equal(np_(K.price(inst)), np_(K.price(inst, cfg=N.SdemcCfg(interleave=2))))
+    ex = N.SdemcCfg(flags=N.CFG_EXACT_EULER)
+    ex2 = N.SdemcCfg(flags=N.CFG_EXACT_EULER, interleave=2)
+    np.testing.assert_array_equal(np_(K.price(inst, cfg=ex)), np_(K.price(inst, cfg=ex2)))
 
 
 def test_exact_euler_variant_replays_reference_order(oracle_mod):
