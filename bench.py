@@ -261,7 +261,7 @@ def run_reference(args):
     value = 1.0 / sec_per_price
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec_per_price * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "config": {"workload": WORKLOAD, "form": "plain run_mc per request"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": "%d stream requests (pilot + main, plain estimator) on %d threads; main "
@@ -432,7 +432,9 @@ def bench_batched_mix(steps, warmup):
     work = sum(m.paths * (m.solver.num_steps + float(m.solver.sde.jump_rate())) for m in mix)
     return {"workload": MIX_WORKLOAD, "instances": n, "steps": steps,
             "batched": {"prices_per_s": n / (batched_ms * 1e-3), "ms_per_mix": batched_ms,
-                        "launch": {"block_threads": tune["choice"][0], "side_streams": tune["choice"][1]},
+                        "launch": {"block_threads": tune["choice"][0], "side_streams": tune["choice"][1],
+                                   "paths_per_lane_by_class": tune["choice"][2] if len(tune["choice"]) > 2 else None,
+                                   "classes": ["d%d" % c.dim for c in plan.classes[:plan.header.n_class]]},
                         "graph": True, "gpu_launches_per_mix": 1 + 1 + len(plan.classes[:plan.header.n_class])},
             "plain_one_per_launch": {"prices_per_s": n / (plain_ms * 1e-3), "ms_per_mix": plain_ms,
                                      "gpu_launches_per_mix": 2 * n},

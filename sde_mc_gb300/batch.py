@@ -9,8 +9,8 @@ kernels + reduction) can be captured once in a CUDA graph and replayed after
 editing path offsets in place (:meth:`BatchPlan.set_path_offsets`).
 
 ``autotune`` is the project's launch-shape tuner: it times the plan under a
-few CTA sizes and side-stream counts and caches the winner per batch
-signature (a JSON file under ``$SDEMC_CACHE_DIR``, default
+few CTA sizes and side-stream counts, then chooses one or two paths per lane
+for each class, and caches the winner per batch signature (a JSON file under ``$SDEMC_CACHE_DIR``, default
 ``~/.cache/sde_mc_gb300``).
 """
 import ctypes
@@ -66,9 +66,16 @@ class BatchPlan:
         for j in range(self.n):
             self.plan_insts[j].path_offset = int(offsets[self.order[j]])
 
-    def set_config(self, block_threads=0, n_side=0):
+    def set_config(self, block_threads=0, n_side=0, interleave=None):
+        """CTA size and side streams for every class; ``interleave[j]`` = paths
+        per lane (1 or 2) of class j."""
         nc = max(self.header.n_class, 1)
-        self.cfgs = (N.SdemcCfg * nc)(*[N.SdemcCfg(block_threads=block_threads) for _ in range(nc)])
+        il = [1] * nc if interleave is None else [int(v) for v in interleave]
+        if len(il) != nc:
+            raise ValueError("interleave needs one entry per class (%d)" % nc)
+        self.cfgs = (N.SdemcCfg * nc)(*[N.SdemcCfg(block_threads=block_threads, interleave=il[j])
+                                        for j in range(nc)])
+        self.interleave = il
         self.n_side = int(n_side)
         while len(self._side) < self.n_side:
             self._side.append(torch.cuda.Stream(device=self.device))
@@ -126,33 +133,49 @@ def _store_cache(cache):
 CANDIDATES = [(128, 0), (64, 0), (256, 0), (128, 4), (128, 8), (64, 8)]
 
 
+def _time_plan(plan, repeats):
+    plan.launch()  # warm
+    ts = []
+    for _ in range(repeats):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        plan.launch()
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return min(ts)
+
+
 def autotune(plan, candidates=CANDIDATES, repeats=2, use_cache=True):
-    """Pick (block_threads, side streams) for this plan by timing each
-    candidate; the choice is cached per batch signature."""
+    """Pick the launch shape for this plan by timing: first (block_threads,
+    side streams) over ``candidates``, then, class by class, two paths per
+    lane instead of one where that makes the whole batch faster (greedy, a
+    1% margin).  The choice is cached per batch signature."""
     sig = plan.signature()
     cache = _load_cache() if use_cache else {}
+    nc = max(plan.header.n_class, 1)
     if sig in cache:
-        bt, ns = cache[sig]["choice"]
-        plan.set_config(bt, ns)
+        choice = cache[sig]["choice"]
+        il = choice[2] if len(choice) > 2 and len(choice[2]) == nc else None
+        plan.set_config(choice[0], choice[1], il)
         return cache[sig]
     plan.upload()
     results = []
     for bt, ns in candidates:
         plan.set_config(bt, ns)
-        plan.launch()  # warm
-        ts = []
-        for _ in range(repeats):
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            plan.launch()
-            e1.record()
-            torch.cuda.synchronize()
-            ts.append(e0.elapsed_time(e1))
-        results.append((min(ts), bt, ns))
+        results.append((_time_plan(plan, repeats), bt, ns))
     results.sort()
-    best = results[0]
-    plan.set_config(best[1], best[2])
-    entry = {"choice": [best[1], best[2]], "ms": best[0], "tried": [[t, b, s] for t, b, s in results]}
+    best_ms, bt, ns = results[0]
+    il = [1] * nc
+    for j in range(nc):
+        trial = list(il)
+        trial[j] = 2
+        plan.set_config(bt, ns, trial)
+        t = _time_plan(plan, repeats)
+        if t < 0.99 * best_ms:
+            il, best_ms = trial, t
+    plan.set_config(bt, ns, il)
+    entry = {"choice": [bt, ns, il], "ms": best_ms, "tried": [[t, b, s] for t, b, s in results]}
     if use_cache:
         cache[sig] = entry
         _store_cache(cache)

@@ -83,6 +83,33 @@ def test_batch_reports_overflow_per_instance():
     assert got[1, 5] == N.EOVERFLOW
 
 
+@pytest.mark.parametrize("bt", [64, 128, 256])
+def test_two_paths_per_lane_batch_is_bit_identical(bt):
+    """Paths-per-thread tiling in K8 (both chunks of a pair in one instance
+    step together; pairs across an instance boundary run one after the
+    other): every instance's result equals pricing it alone."""
+    insts = B.lower_mix(small_mix(24))
+    ref = alone(insts)
+    plan = B.BatchPlan(insts)
+    nc = plan.header.n_class
+    for il in ([2] * nc, [1 + (j % 2) for j in range(nc)]):
+        plan.set_config(bt, 2, il)
+        np.testing.assert_array_equal(plan.run().cpu().numpy(), ref)
+
+
+def test_batch_overflow_with_two_paths_per_lane():
+    ok = inst_for(merton1d(50), num_paths=1000, seed=1)
+    bad = inst_for(merton1d(50), num_paths=1000, seed=1)
+    bad.rate = 5000.0
+    bad.inv_rate = 2e-8
+    bad.num_steps = 1
+    plan = B.BatchPlan([ok, bad, ok])
+    plan.set_config(128, 0, [2] * plan.header.n_class)
+    got = plan.run().cpu().numpy()
+    assert got[0, 5] == 0 and got[2, 5] == 0
+    assert got[1, 5] == N.EOVERFLOW
+
+
 def test_autotune_choice_gives_same_bits(tmp_path, monkeypatch):
     monkeypatch.setenv("SDEMC_CACHE_DIR", str(tmp_path))
     insts = B.lower_mix(small_mix(16))
