@@ -65,9 +65,12 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--plain-windows", type=int, default=10,
                     help="windows of the stream the plain one-request-per-launch server replays")
-    ap.add_argument("--sections", default="rainbow,mlmc,mix,cv,accuracy",
-                    help="extra sections measured once: rainbow, mlmc, mix, cv, accuracy (comma list, "
-                         "or 'none')")
+    ap.add_argument("--sections", default="rainbow,materialise,mlmc,mix,cv,accuracy",
+                    help="extra sections measured once: rainbow, materialise, mlmc, mix, cv, accuracy "
+                         "(comma list, or 'none')")
+    ap.add_argument("--profile-store", type=int, default=0,
+                    help="profiling driver: materialise this many 2D rainbow paths (K4, AdaptedPathData "
+                         "layout) three times, then exit")
     ap.add_argument("--profile-paths", type=int, default=0,
                     help="profiling driver: three 2D-rainbow price launches at this many paths, then exit")
     ap.add_argument("--profile-serve", type=float, default=0.0,
@@ -355,6 +358,60 @@ def bench_rainbow_plain(dev, steps, warmup, fp32_peak, mufu_peak):
                                   "ops_per_path_step": mufu_per_path_step(2, 2.0 / steps_per_path),
                                   "peak_source": "measured rsqrt.approx probe (sdemc_mufu_probe)"}},
             "l2": "flushed (256 MB write) between timed steps", "gpu_launches": 2 * steps}
+
+
+def bench_materialise(dev, hbm_peak):
+    """Materialised mode (K4): the 2D rainbow's paths in the AdaptedPathData
+    layout (paths, left limits, time, jumps: S + 1 rows; normals: S rows),
+    2^20 paths, timed on the kernel alone; HBM roofline of the stores."""
+    import ctypes
+    import torch
+    from sde_mc_gb300 import _native as N
+    from sde_mc_gb300.lowering import lower
+    solver, payoff, disc = make_problem()
+    n, d = 1 << 20, 2
+    S = solver.num_steps + solver.max_jumps
+    f32 = dict(dtype=torch.float32, device=dev)
+    bufs = {"paths": torch.empty((n, S + 1, d), **f32), "left": torch.empty((n, S + 1, d), **f32),
+            "time": torch.empty((n, S + 1), **f32), "jumps": torch.empty((n, S + 1, d), **f32),
+            "normals": torch.empty((n, S, d), **f32), "payoffs": torch.empty(n, **f32),
+            "steps": torch.empty(n, dtype=torch.int32, device=dev)}
+    nbytes = sum(b.numel() * b.element_size() for b in bufs.values())
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    lib = N.load()
+    s = N.stream_handle(dev)
+
+    def run(i):
+        inst = lower(solver, payoff, disc, num_paths=n, path_offset=(i + 1) * n, seed=3)
+        g = bufs.get
+        N.check(lib.sdemc_materialise(ctypes.byref(inst), S, N.ptr(g("paths")), N.ptr(g("left")),
+                                      N.ptr(g("time")), N.ptr(g("jumps")), N.ptr(g("normals")),
+                                      N.ptr(g("payoffs")), N.ptr(g("steps")), None, 0, None, None, None, 0,
+                                      N.ptr(status), s), "materialise")
+
+    for i in range(3):
+        run(i)
+    torch.cuda.synchronize()
+    ms = []
+    for i in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        run(3 + i)
+        e1.record()
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    N.status_error(int(status.item()), "materialise")
+    t = statistics.mean(ms) * 1e-3
+    executed = float(bufs["steps"].double().sum())
+    gbs = nbytes / t / 1e9
+    return {"workload": "2D rainbow, 2^20 paths, AdaptedPathData layout at %d step rows" % S,
+            "bytes_written": nbytes, "ms": t * 1e3, "path_steps_per_s": executed / t,
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": gbs / hbm_peak if hbm_peak else None,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy, read + write)",
+                         "bytes": "the layout's arrays: (S + 1) rows x (3d + 1) floats + S rows x d floats "
+                                  "per path, + payoff and step count"},
+            "l2": "outputs (%.1f GB) far larger than L2" % (nbytes / 1e9)}
 
 
 def bench_rainbow_mlmc(dev):
@@ -689,6 +746,20 @@ def profile_cv(n):
                       "grad_norm": float(cv.grad.norm())}))
 
 
+def profile_store(n):
+    import torch
+    from sde_mc_gb300 import kernels as K
+    from sde_mc_gb300.lowering import lower
+    solver, payoff, disc = make_problem()
+    S = solver.num_steps + solver.max_jumps
+    for i in range(3):
+        m = K.materialise(lower(solver, payoff, disc, num_paths=n, path_offset=i * n, seed=3), S,
+                          want=("paths", "left", "time", "jumps", "normals", "payoffs", "steps"))
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_store": n, "status": int(m["status"].item()),
+                      "steps_mean": float(m["steps"].double().mean())}))
+
+
 def profile_launches(n):
     import torch
     from sde_mc_gb300 import kernels as K
@@ -713,6 +784,8 @@ def main():
         return run_reference(args)
     if args.profile_paths:
         return profile_launches(args.profile_paths)
+    if args.profile_store:
+        return profile_store(args.profile_store)
     if args.profile_serve:
         return profile_serve(args.profile_serve)
     if args.profile_cv:
@@ -790,6 +863,9 @@ def main():
         secs = [s.strip() for s in args.sections.split(",") if s.strip() and s.strip() != "none"]
         if "rainbow" in secs:
             line["rainbow2d_plain"] = _section(bench_rainbow_plain, dev, 20, 5, fp32_peak, mufu_peak)
+        if "materialise" in secs:
+            peaks = load_json_file("MEASURED_PEAKS.json") or {}
+            line["materialised_mode"] = _section(bench_materialise, dev, peaks.get("hbm_gbs"))
         if "mlmc" in secs:
             line["rainbow2d_mlmc"] = _section(bench_rainbow_mlmc, dev)
         if "mix" in secs:
