@@ -16,6 +16,121 @@ struct StoreParams {
   RoundKeys rk;
 };
 
+// AdaptedPathData stores through shared memory.  A path's rows are contiguous
+// in every array, so a lane writing its own row at each step touches one
+// 32-byte sector per lane and array for a few bytes; instead each lane
+// parks kT steps of (paths, left, jumps, time, normals) in its warp's tile and
+// the warp then writes lane after lane's kT-row segments with consecutive
+// lanes on consecutive addresses (full sectors, a few lines per store
+// instruction).  The padding rows after the loop (the terminal state repeated
+// to S, zero normals) go the same way.  Called in lock-step: k is the same in
+// every lane of the warp.
+template <int D, int NW>
+struct TiledStoreSink {
+  static constexpr bool kWantsLeft = true;
+  static constexpr int kT = (16 / D) > 2 ? 16 / D : 2;  // rows per tile: >= 64 B of a path's state
+  static constexpr int kRowW = 3 * D + 1;             // paths, left, jumps (D each), time
+  static constexpr int kNw = D * NW;                  // normals per step
+  static constexpr int kW = kRowW + kNw;
+  static constexpr int kTileFloats = kT * 32 * kW;
+  float *paths, *left, *time, *jumps, *normals;
+  float* tile;       // this warp's kT x 32 x kW floats
+  int64_t p0;        // path of lane 0
+  int64_t n;         // num_paths
+  int S;
+
+  SDEMC_DI float& at(int kk, int lane, int f) const { return tile[(kk * 32 + lane) * kW + f]; }
+
+  template <int Dd> SDEMC_DI void init(const float* x) {
+    const int64_t p = p0 + (threadIdx.x & 31);
+    if (p >= n) return;
+    const size_t row = (size_t)p * (S + 1);
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      if (paths) paths[row * D + i] = x[i];
+      if (left) left[row * D + i] = x[i];
+      if (jumps) jumps[row * D + i] = 0.f;
+    }
+    if (time) time[row] = 0.f;
+  }
+
+  // One array's segments: every lane's rows [r0, r0 + cnt) of width w, from
+  // tile column f0 on.
+  SDEMC_DI void put(float* base, int rows, int w, int f0, int r0, int cnt) const {
+    if (!base) return;
+    const int lane = threadIdx.x & 31;
+    const int seg = cnt * w;
+    for (int e = lane; e < 32 * seg; e += 32) {
+      const int j = e / seg, r = e - j * seg, kk = r / w, f = r - kk * w;
+      const int64_t p = p0 + j;
+      if (p < n) base[((size_t)p * rows + r0 + kk) * w + f] = at(kk, j, f0 + f);
+    }
+  }
+
+  SDEMC_DI void flush(int k0, int cnt) const {
+    __syncwarp();
+    put(paths, S + 1, D, 0, k0 + 1, cnt);
+    put(left, S + 1, D, D, k0 + 1, cnt);
+    put(jumps, S + 1, D, 2 * D, k0 + 1, cnt);
+    put(time, S + 1, 1, 3 * D, k0 + 1, cnt);
+    put(normals, S, kNw, kRowW, k0, cnt);
+    __syncwarp();
+  }
+
+  template <int Dd, int NWd>
+  SDEMC_DI void step(int k, const float* xl, const float* x, float t, float J, int sel,
+                     const float* dW, const float* dW2, const float*, int jump_one) {
+    if (k >= S) return;
+    const int lane = threadIdx.x & 31, kk = k % kT;
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      at(kk, lane, i) = x[i];
+      at(kk, lane, D + i) = xl[i];
+      at(kk, lane, 2 * D + i) = (jump_one && i != sel) ? 0.f : J;
+      if (NW == 1) {
+        at(kk, lane, kRowW + i) = dW[i];
+      } else {
+        at(kk, lane, kRowW + 2 * i) = dW[i];
+        at(kk, lane, kRowW + 2 * i + 1) = dW2[i];
+      }
+    }
+    at(kk, lane, 3 * D) = t;
+    if (kk == kT - 1) flush(k - kk, kT);
+  }
+
+  // Rows kend .. S-1: the rest of the last tile, then the terminal state (x,
+  // x, 0, t) repeated with zero normals, tile by tile.
+  template <int Dd, int NWd>
+  SDEMC_DI void finish(int kend, const float* x, float t) {
+    const int lane = threadIdx.x & 31;
+    if (kend > S) kend = S;
+    int k = kend;
+    if (k % kT != 0) {
+      // complete the open tile with padding rows, then write it
+      const int k0 = k - k % kT;
+      const int stop = min(S, k0 + kT);
+      for (; k < stop; ++k) fill_row(k % kT, lane, x, t);
+      flush(k0, stop - k0);
+    }
+    if (k < S) {
+      for (int kk = 0; kk < kT; ++kk) fill_row(kk, lane, x, t);
+      for (; k < S; k += kT) flush(k, min(kT, S - k));
+    }
+  }
+
+  SDEMC_DI void fill_row(int kk, int lane, const float* x, float t) const {
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      at(kk, lane, i) = x[i];
+      at(kk, lane, D + i) = x[i];
+      at(kk, lane, 2 * D + i) = 0.f;
+    }
+    at(kk, lane, 3 * D) = t;
+#pragma unroll
+    for (int i = 0; i < kNw; ++i) at(kk, lane, kRowW + i) = 0.f;
+  }
+};
+
 template <int D, int NOISE, int MODE>
 __global__ void __launch_bounds__(128)
 materialise_kernel(const __grid_constant__ StoreParams P, int S, float* paths, float* left,
@@ -23,27 +138,41 @@ materialise_kernel(const __grid_constant__ StoreParams P, int S, float* paths, f
                    float* zout, int zdim, float* jt, float* jm, int32_t* jsel, int jcap,
                    int32_t* status, int max_iters) {
   using L = Layout<D, NOISE>;
+  using Tiled = TiledStoreSink<D, L::NW>;
+  __shared__ float tiles[4][Tiled::kTileFloats];
   const sdemc_inst& I = P.I;
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = p < I.num_paths;
-  StoreSink sk{};
-  sk.S = S;
-  sk.zdim = zdim;
-  if (valid) {
-    const size_t row = (size_t)p * (S + 1);
-    sk.paths = paths ? paths + row * D : nullptr;
-    sk.left = left ? left + row * D : nullptr;
-    sk.time = time ? time + row : nullptr;
-    sk.jumps = jumps ? jumps + row * D : nullptr;
-    sk.normals = normals ? normals + (size_t)p * S * D * L::NW : nullptr;
-    sk.z = zout ? zout + (size_t)p * S * zdim : nullptr;
-  }
   NativeDraws<D, NOISE> dr;
   dr.init(I, (uint64_t)p, ConstKeys{&P.rk});
   bool ovf = false;
   float x[D];
   const int it = max_iters < S ? max_iters : S;
-  const int own = simulate<D, NOISE, MODE>(I, dr, sk, x, it, ovf);
+  int own;
+  if (!zout) {
+    Tiled sk;
+    sk.paths = paths; sk.left = left; sk.time = time; sk.jumps = jumps; sk.normals = normals;
+    sk.tile = tiles[threadIdx.x >> 5];
+    sk.p0 = p - (threadIdx.x & 31);
+    sk.n = I.num_paths;
+    sk.S = S;
+    own = simulate<D, NOISE, MODE>(I, dr, sk, x, it, ovf);
+  } else {
+    // with the raw draws exported (the oracle's step-by-step check): per-lane rows
+    StoreSink sk{};
+    sk.S = S;
+    sk.zdim = zdim;
+    if (valid) {
+      const size_t row = (size_t)p * (S + 1);
+      sk.paths = paths ? paths + row * D : nullptr;
+      sk.left = left ? left + row * D : nullptr;
+      sk.time = time ? time + row : nullptr;
+      sk.jumps = jumps ? jumps + row * D : nullptr;
+      sk.normals = normals ? normals + (size_t)p * S * D * L::NW : nullptr;
+      sk.z = zout + (size_t)p * S * zdim;
+    }
+    own = simulate<D, NOISE, MODE>(I, dr, sk, x, it, ovf);
+  }
   if (!valid) return;
   if (payoffs) payoffs[p] = __fmul_rn(payoff<D>(I, x), I.discount);
   if (steps) steps[p] = own;

@@ -145,6 +145,28 @@ def test_materialise_matches_oracle_step_by_step(name, oracle_mod):
         np.testing.assert_array_equal(g[key], ref[key], err_msg=key)
 
 
+@pytest.mark.parametrize("name", list(EXPORT_CASES))
+def test_tiled_stores_equal_per_lane_stores(name):
+    """K4 writes through shared-memory tiles (coalesced segments) unless the
+    raw draws are exported; both give the same AdaptedPathData bits, with the
+    step cap odd, exact and short of the loop (overflow)."""
+    case = EXPORT_CASES[name]()
+    solver = case[0]
+    base = solver.num_steps + solver.max_jumps + 3 if is_adapted(case) else solver.num_steps
+    for S, n in ((base, 777), (base + 5, 130), (max(solver.num_steps // 2, 1), 64)):
+        if not is_adapted(case) and S < solver.num_steps:
+            continue
+        inst = inst_for(case, num_paths=n, seed=19, path_offset=3)
+        a = K.materialise(inst, S)
+        b = K.materialise(inst, S, export_draws=True, jcap=0)
+        for key in ("paths", "left", "time", "jumps", "normals", "payoffs", "steps", "status"):
+            np.testing.assert_array_equal(np_(a[key]), np_(b[key]), err_msg="%s S=%d" % (key, S))
+
+
+def is_adapted(case):
+    return hasattr(case[0], "max_jumps")
+
+
 @pytest.mark.parametrize("name", ["merton1d", "indep2d", "levy2d", "basket5", "double_gbm", "heston"])
 def test_native_draws_match_oracle_transforms(name, oracle_mod):
     """Philox words are bit-exact (above); the MUFU-based Box-Muller and the
