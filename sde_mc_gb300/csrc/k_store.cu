@@ -32,14 +32,15 @@ struct TiledStoreSink {
   static constexpr int kRowW = 3 * D + 1;             // paths, left, jumps (D each), time
   static constexpr int kNw = D * NW;                  // normals per step
   static constexpr int kW = kRowW + kNw;
-  static constexpr int kTileFloats = kT * 32 * kW;
+  static constexpr int kLaneStride = kT * kW + 1;  // odd: a lane's writes and the flush reads spread over banks
+  static constexpr int kTileFloats = 32 * kLaneStride;
   float *paths, *left, *time, *jumps, *normals;
-  float* tile;       // this warp's kT x 32 x kW floats
+  float* tile;       // this warp's 32 lanes x (kT x kW + 1) floats
   int64_t p0;        // path of lane 0
   int64_t n;         // num_paths
   int S;
 
-  SDEMC_DI float& at(int kk, int lane, int f) const { return tile[(kk * 32 + lane) * kW + f]; }
+  SDEMC_DI float& at(int kk, int lane, int f) const { return tile[lane * kLaneStride + kk * kW + f]; }
 
   template <int Dd> SDEMC_DI void init(const float* x) {
     const int64_t p = p0 + (threadIdx.x & 31);
@@ -54,26 +55,30 @@ struct TiledStoreSink {
     if (time) time[row] = 0.f;
   }
 
-  // One array's segments: every lane's rows [r0, r0 + cnt) of width w, from
-  // tile column f0 on.
-  SDEMC_DI void put(float* base, int rows, int w, int f0, int r0, int cnt) const {
+  // One array's segments: every lane's rows [r0, r0 + cnt) of width W, from
+  // tile column f0 on.  CNT > 0: a full tile (cnt = CNT, so the index
+  // arithmetic divides by constants); CNT = 0: a partial tile of cnt rows.
+  template <int W, int CNT>
+  SDEMC_DI void put(float* base, int rows, int f0, int r0, int cnt) const {
     if (!base) return;
     const int lane = threadIdx.x & 31;
-    const int seg = cnt * w;
+    const int seg = (CNT > 0 ? CNT : cnt) * W;
+#pragma unroll 4
     for (int e = lane; e < 32 * seg; e += 32) {
-      const int j = e / seg, r = e - j * seg, kk = r / w, f = r - kk * w;
+      const int j = e / seg, r = e - j * seg, kk = r / W, f = r - kk * W;
       const int64_t p = p0 + j;
-      if (p < n) base[((size_t)p * rows + r0 + kk) * w + f] = at(kk, j, f0 + f);
+      if (p < n) base[((size_t)p * rows + r0 + kk) * W + f] = at(kk, j, f0 + f);
     }
   }
 
+  template <int CNT>
   SDEMC_DI void flush(int k0, int cnt) const {
     __syncwarp();
-    put(paths, S + 1, D, 0, k0 + 1, cnt);
-    put(left, S + 1, D, D, k0 + 1, cnt);
-    put(jumps, S + 1, D, 2 * D, k0 + 1, cnt);
-    put(time, S + 1, 1, 3 * D, k0 + 1, cnt);
-    put(normals, S, kNw, kRowW, k0, cnt);
+    put<D, CNT>(paths, S + 1, 0, k0 + 1, cnt);
+    put<D, CNT>(left, S + 1, D, k0 + 1, cnt);
+    put<D, CNT>(jumps, S + 1, 2 * D, k0 + 1, cnt);
+    put<1, CNT>(time, S + 1, 3 * D, k0 + 1, cnt);
+    put<kNw, CNT>(normals, S, kRowW, k0, cnt);
     __syncwarp();
   }
 
@@ -95,7 +100,7 @@ struct TiledStoreSink {
       }
     }
     at(kk, lane, 3 * D) = t;
-    if (kk == kT - 1) flush(k - kk, kT);
+    if (kk == kT - 1) flush<kT>(k - kk, kT);
   }
 
   // Rows kend .. S-1: the rest of the last tile, then the terminal state (x,
@@ -110,11 +115,12 @@ struct TiledStoreSink {
       const int k0 = k - k % kT;
       const int stop = min(S, k0 + kT);
       for (; k < stop; ++k) fill_row(k % kT, lane, x, t);
-      flush(k0, stop - k0);
+      flush<0>(k0, stop - k0);
     }
     if (k < S) {
       for (int kk = 0; kk < kT; ++kk) fill_row(kk, lane, x, t);
-      for (; k < S; k += kT) flush(k, min(kT, S - k));
+      for (; k + kT <= S; k += kT) flush<kT>(k, kT);
+      if (k < S) flush<0>(k, S - k);
     }
   }
 
