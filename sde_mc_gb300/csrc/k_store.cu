@@ -62,6 +62,24 @@ struct TiledStoreSink {
   SDEMC_DI void put(float* base, int rows, int f0, int r0, int cnt) const {
     if (!base) return;
     const int lane = threadIdx.x & 31;
+    constexpr int SEG = CNT * W;
+    if (CNT > 0 && SEG <= 32 && (32 % (SEG > 0 ? SEG : 1)) == 0) {
+      // a full tile whose segments tile the warp: every lane keeps one
+      // (row, column) of the segment and walks the paths
+      constexpr int PPI = 32 / (SEG > 0 ? SEG : 1);  // paths per store instruction
+      const int q = lane % SEG, kk = q / W, f = q - kk * W;
+      const int jl = lane / SEG;
+      const int soff = kk * kW + f0 + f;
+      float* dst = base + ((size_t)(p0 + jl) * rows + r0 + kk) * W + f;
+      const size_t step = (size_t)PPI * rows * W;
+#pragma unroll
+      for (int it = 0; it < SEG; ++it) {
+        const int j = it * PPI + jl;
+        if (p0 + j < n) *dst = tile[j * kLaneStride + soff];
+        dst += step;
+      }
+      return;
+    }
     const int seg = (CNT > 0 ? CNT : cnt) * W;
 #pragma unroll 4
     for (int e = lane; e < 32 * seg; e += 32) {
