@@ -191,7 +191,7 @@ struct DeltaCvSink {
 };
 
 template <int D, int NOISE, int MODE, int KIND>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 3)
 serve_kernel(const __grid_constant__ ServeParams P) {
   __shared__ sdemc_inst s_inst[kServeMaxWarps];
   __shared__ float s_beta[kServeMaxWarps][2 * D + 1];
