@@ -11,7 +11,7 @@ import torch
 import sde_mc_gb300 as sm
 from sde_mc_gb300 import _native as N
 from sde_mc_gb300.lowering import lower, max_jumps_for
-from tests.cases import FIXTURE_CASES, inst_for, indep2d, merton1d
+from tests.cases import FIXTURE_CASES, inst_for, indep2d, levy2d, merton1d
 from tests.conftest import ROOT, load_npz
 
 
@@ -302,3 +302,34 @@ def test_heston_and_asian_lowering():
     assert e.model == N.MODEL_AFFINE and e.diff_q[0] == np.sqrt(f(0.04)) and e.diff_q[1] == 0.0
     with pytest.raises(NotImplementedError):
         lower(sm.HestonSolver(sm.Gbm(0.02, 0.2, torch.ones(2), 2), 1.0, 10), sm.EuroCall(1.0), None)
+
+
+def test_descriptor_and_launch_validation_on_the_host():
+    """Bad descriptors and launch shapes are refused before any device work
+    (no GPU needed): model kinds outside their shapes, interleave values."""
+    import ctypes
+    from tests.cases import asian_merton, heston
+    lib = N.load()
+    fake = ctypes.c_void_p(256)  # never dereferenced: validation fails first
+    out = ctypes.c_void_p(512)
+
+    def price_rc(inst, cfg=None):
+        return lib.sdemc_price_chunks(ctypes.byref(inst), N.byref(cfg), fake, 1 << 30, None, None)
+
+    h = inst_for(heston(24), num_paths=64)
+    h.grid = N.GRID_ADAPTED
+    assert price_rc(h) == N.EUNSUPPORTED            # Heston steps on the uniform grid only
+    a = inst_for(asian_merton(20), num_paths=64)
+    a.dim = 3
+    assert price_rc(a) == N.EUNSUPPORTED            # the Asian wrapper is 2-D
+    a = inst_for(asian_merton(20), num_paths=64)
+    a.model = 7
+    assert price_rc(a) == N.EINVAL                  # unknown model kind
+    ok = inst_for(merton1d(10), num_paths=64)
+    assert price_rc(ok, N.SdemcCfg(interleave=3)) == N.EINVAL
+    assert price_rc(ok, N.SdemcCfg(block_threads=48)) == N.EINVAL
+    f = inst_for(merton1d(10), num_paths=64)
+    assert lib.sdemc_price_f64(ctypes.byref(f), fake, 0, out, None) == N.ENOMEM
+    lv = inst_for(levy2d(8), num_paths=64)
+    assert lib.sdemc_price_f64(ctypes.byref(lv), fake, 1 << 30, out, None) == N.EUNSUPPORTED
+

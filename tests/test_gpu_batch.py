@@ -95,6 +95,8 @@ def test_two_paths_per_lane_batch_is_bit_identical(bt):
     for il in ([2] * nc, [1 + (j % 2) for j in range(nc)]):
         plan.set_config(bt, 2, il)
         np.testing.assert_array_equal(plan.run().cpu().numpy(), ref)
+    with pytest.raises(ValueError):
+        plan.set_config(bt, 2, [2] * (nc + 1))
 
 
 def test_batch_overflow_with_two_paths_per_lane():
