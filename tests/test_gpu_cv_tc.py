@@ -91,3 +91,19 @@ def test_tc_backward_large_batch_and_index(d):
     parts = np.split(g_mma, np.cumsum(sizes)[:-1])
     for i, (e, m) in enumerate(_layer_norms(g_tc, parts)):
         assert e <= 5e-3 * m + 1e-9, (i, e / m)
+
+
+def test_tc_backward_small_batches_match_mma():
+    """Minibatches smaller than a 128-path group and step counts shorter than
+    one 32-step range: padded rows contribute nothing."""
+    fx, data, params = _fixture()
+    n, S, d = fx["normals"].shape
+    cv = V.GpuCv(_net(d, params), d, DEV)
+    for m in (1, 3, 127, 129):
+        idx = torch.arange(m, device=DEV) % n
+        gamma = cv.forward(data, float(fx["r"]), idx)
+        g_tc = cv.backward_tc(data, float(fx["r"]), gamma, idx).cpu().numpy().copy()
+        assert int(cv._bwd_status.item()) == 0
+        g_mma = cv.backward(data, float(fx["r"]), gamma, idx).cpu().numpy().copy()
+        assert np.isfinite(g_tc).all()
+        assert np.linalg.norm(g_tc - g_mma) <= 5e-3 * np.linalg.norm(g_mma) + 1e-9, m

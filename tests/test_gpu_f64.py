@@ -56,3 +56,13 @@ def test_fp64_is_deterministic_and_rejects_unsupported():
     assert a == b
     with pytest.raises(Exception):
         K.price_f64(inst_for(levy2d(8), num_paths=64))
+
+
+def test_fp64_empty_and_ragged_sizes():
+    for n in (0, 1, 31, 33, 1000):
+        inst = inst_for(merton1d(10), num_paths=n, seed=4)
+        a = K.price(inst).cpu().tolist()
+        b = K.price_f64(inst).cpu().tolist()
+        assert b[5] == 0 and b[2] == n == a[2]
+        if n > 1:
+            assert abs(a[3] - b[3]) <= 1e-4 * abs(b[3]) + 1e-7
