@@ -17,9 +17,17 @@ descriptor travels as a CPU ``uint8`` tensor holding the bytes of one
 * ``sdemc::adam_step(params!, grad, m!, v!, step, lr, beta1, beta2, eps)`` — one
   torch.optim.Adam step in place.
 * ``sdemc::philox(seed, stream_id, tag, path, first_block, nblocks)`` -> i32[nblocks, 4].
+* ``sdemc::price_f64(inst)`` -> f64[6] — K11, the FP64 run on the same paths.
+* ``sdemc::materialise(inst, steps_cap)`` -> (paths, left, time, jumps, normals,
+  payoffs, steps, status) — K4, ``solve`` with storage (sde_mc/solvers.py:150-226).
+* ``sdemc::replay(inst, dw, jump_times, marks, asset)`` -> (paths, left, time,
+  jumps, payoffs, steps, status) — K3, the loop on recorded draws.
+* ``sdemc::cv_backward_tc(...)`` — K6 on tcgen05, arguments as ``cv_backward``.
+* ``sdemc::price_cv(inst, params, disc_rate)`` -> f64[8] — K7, ``mc_apply_cvs``
+  for a trained network (sde_mc/mc.py:214-243).
 """
 import ctypes
-from typing import Optional
+from typing import Optional, Tuple
 
 import torch
 
@@ -158,4 +166,93 @@ def _(seed, stream_id, tag, path, first_block, nblocks):
     return torch.empty((nblocks, 4), dtype=torch.int32, device="cuda")
 
 
-OPS = ("price", "mlmc_level", "cv_forward", "cv_backward", "adam_step", "philox")
+@torch.library.custom_op("sdemc::price_f64", mutates_args=())
+def price_f64(inst: torch.Tensor) -> torch.Tensor:
+    return K.price_f64(_inst(inst))
+
+
+@price_f64.register_fake
+def _(inst):
+    return torch.empty(6, dtype=torch.float64, device="cuda")
+
+
+_STORE = ("paths", "left", "time", "jumps", "normals", "payoffs", "steps", "status")
+_T8 = Tuple[torch.Tensor, torch.Tensor, torch.Tensor, torch.Tensor, torch.Tensor, torch.Tensor, torch.Tensor,
+            torch.Tensor]
+
+
+@torch.library.custom_op("sdemc::materialise", mutates_args=())
+def materialise(inst: torch.Tensor, steps_cap: int) -> _T8:
+    out = K.materialise(_inst(inst), int(steps_cap))
+    return tuple(out[k] for k in _STORE)
+
+
+def _store_fakes(I, S, n):
+    d = int(I.dim)
+    nw = 1 if I.noise == N.NOISE_DIAG else 2
+    f = dict(dtype=torch.float32, device="cuda")
+    return (torch.empty((n, S + 1, d), **f), torch.empty((n, S + 1, d), **f), torch.empty((n, S + 1), **f),
+            torch.empty((n, S + 1, d), **f), torch.empty((n, S, d) if nw == 1 else (n, S, d, 2), **f),
+            torch.empty(n, **f), torch.empty(n, dtype=torch.int32, device="cuda"),
+            torch.empty(1, dtype=torch.int32, device="cuda"))
+
+
+@materialise.register_fake
+def _(inst, steps_cap):
+    I = _inst(inst)
+    return _store_fakes(I, int(steps_cap), int(I.num_paths))
+
+
+@torch.library.custom_op("sdemc::replay", mutates_args=())
+def replay(inst: torch.Tensor, dw: torch.Tensor, jump_times: Optional[torch.Tensor], marks: Optional[torch.Tensor],
+           asset: Optional[torch.Tensor]) -> Tuple[torch.Tensor, torch.Tensor, torch.Tensor, torch.Tensor,
+                                                   torch.Tensor, torch.Tensor, torch.Tensor]:
+    _check(dw, "dw", torch.float32)
+    out = K.replay(_inst(inst), dw, jump_times, marks, asset)
+    return tuple(out[k] for k in ("paths", "left", "time", "jumps", "payoffs", "steps", "status"))
+
+
+@replay.register_fake
+def _(inst, dw, jump_times, marks, asset):
+    I = _inst(inst)
+    bs, S = int(dw.shape[0]), int(dw.shape[1])
+    p, l, t, j, _, pay, st, stat = _store_fakes(I, S, bs)
+    return p, l, t, j, pay, st, stat
+
+
+@torch.library.custom_op("sdemc::cv_backward_tc", mutates_args=())
+def cv_backward_tc(params: torch.Tensor, time: torch.Tensor, paths: torch.Tensor, normals: torch.Tensor,
+                   gamma: torch.Tensor, index: Optional[torch.Tensor], rate: float) -> torch.Tensor:
+    d, S, n = _cv_args(params, time, paths, normals, index)
+    _check(gamma, "gamma", torch.float32, 1)
+    if gamma.numel() != n:
+        raise ValueError("gamma must hold one value per selected path")
+    nparts = 2 * _sms()
+    partials = torch.empty((nparts, params.numel()), dtype=torch.float32, device=params.device)
+    grad = torch.empty_like(params)
+    status = torch.zeros(1, dtype=torch.int32, device=params.device)
+    rc = N.load().sdemc_cv_backward_tc(d, N.ptr(params), N.ptr(time), N.ptr(paths), N.ptr(normals), N.ptr(index),
+                                       n, S, float(rate), N.ptr(gamma), N.ptr(partials), nparts, N.ptr(grad),
+                                       N.ptr(status), N.stream_handle(params.device))
+    N.check(rc, "sdemc_cv_backward_tc")
+    return grad
+
+
+@cv_backward_tc.register_fake
+def _(params, time, paths, normals, gamma, index, rate):
+    return torch.empty_like(params)
+
+
+@torch.library.custom_op("sdemc::price_cv", mutates_args=())
+def price_cv(inst: torch.Tensor, params: torch.Tensor, disc_rate: float) -> torch.Tensor:
+    _check(params, "params", torch.float32, 1)
+    return K.price_cv(_inst(inst), params, float(disc_rate))
+
+
+@price_cv.register_fake
+def _(inst, params, disc_rate):
+    return torch.empty(8, dtype=torch.float64, device="cuda")
+
+
+OPS = ("price", "price_f64", "mlmc_level", "materialise", "replay", "cv_forward", "cv_backward", "cv_backward_tc",
+       "price_cv", "adam_step", "philox")
