@@ -281,6 +281,23 @@ int sdemc_price_batch(const void* h_blob, const void* d_blob, void* d_scratch,
                       size_t scratch_bytes, double* d_out, const sdemc_cfg* h_cfgs,
                       void* const* side_streams, int n_side, void* stream);
 
+/* The project's launch-shape autotuner for a planned batch (the plan blob
+ * already on the device): times sdemc_price_batch with CUDA events on
+ * `stream` for every candidate (h_block_threads[c], h_side_counts[c] side
+ * streams out of the max_side given), then tries two paths per lane class by
+ * class, keeping it when the whole batch gets >1% faster.  Writes one
+ * sdemc_cfg per class to h_cfgs (n_class entries), the chosen side-stream
+ * count to *h_n_side, the best time (ms) to *h_ms and, when h_cand_ms is
+ * not null, each candidate's time.  Synchronises the stream; d_out holds the
+ * results of the last timed launch.  No reference counterpart (the
+ * reference prices one problem per call).                                  */
+int sdemc_batch_autotune(const void* h_blob, const void* d_blob, void* d_scratch,
+                         size_t scratch_bytes, double* d_out,
+                         const int32_t* h_block_threads, const int32_t* h_side_counts,
+                         int n_cand, void* const* side_streams, int max_side,
+                         int repeats, sdemc_cfg* h_cfgs, int* h_n_side, float* h_ms,
+                         float* h_cand_ms, void* stream);
+
 /* ---- K3: replay of recorded draws --------------------------------------
  * Runs the reference's jump-adapted loop (sde_mc/solvers.py:164-226, or its
  * uniform-grid twin :68-88) on draws exported from the reference: d_jump_times

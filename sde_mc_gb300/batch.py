@@ -133,24 +133,11 @@ def _store_cache(cache):
 CANDIDATES = [(128, 0), (64, 0), (256, 0), (128, 4), (128, 8), (64, 8)]
 
 
-def _time_plan(plan, repeats):
-    plan.launch()  # warm
-    ts = []
-    for _ in range(repeats):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        plan.launch()
-        e1.record()
-        torch.cuda.synchronize()
-        ts.append(e0.elapsed_time(e1))
-    return min(ts)
-
-
 def autotune(plan, candidates=CANDIDATES, repeats=2, use_cache=True):
-    """Pick the launch shape for this plan by timing: first (block_threads,
-    side streams) over ``candidates``, then, class by class, two paths per
-    lane instead of one where that makes the whole batch faster (greedy, a
-    1% margin).  The choice is cached per batch signature."""
+    """Pick the launch shape for this plan: ``sdemc_batch_autotune`` times
+    every (block_threads, side streams) candidate with CUDA events, then, class
+    by class, two paths per lane instead of one where that makes the whole
+    batch >1% faster.  The choice is cached per batch signature."""
     sig = plan.signature()
     cache = _load_cache() if use_cache else {}
     nc = max(plan.header.n_class, 1)
@@ -160,22 +147,28 @@ def autotune(plan, candidates=CANDIDATES, repeats=2, use_cache=True):
         plan.set_config(choice[0], choice[1], il)
         return cache[sig]
     plan.upload()
-    results = []
-    for bt, ns in candidates:
-        plan.set_config(bt, ns)
-        results.append((_time_plan(plan, repeats), bt, ns))
-    results.sort()
-    best_ms, bt, ns = results[0]
-    il = [1] * nc
-    for j in range(nc):
-        trial = list(il)
-        trial[j] = 2
-        plan.set_config(bt, ns, trial)
-        t = _time_plan(plan, repeats)
-        if t < 0.99 * best_ms:
-            il, best_ms = trial, t
-    plan.set_config(bt, ns, il)
-    entry = {"choice": [bt, ns, il], "ms": best_ms, "tried": [[t, b, s] for t, b, s in results]}
+    nca = len(candidates)
+    bts = (ctypes.c_int32 * nca)(*[c[0] for c in candidates])
+    sides = (ctypes.c_int32 * nca)(*[c[1] for c in candidates])
+    max_side = max(c[1] for c in candidates)
+    plan.set_config(0, max_side)
+    streams = (ctypes.c_void_p * max(max_side, 1))(*[s.cuda_stream for s in plan._side[:max_side]])
+    cfgs = (N.SdemcCfg * nc)()
+    n_side, ms = ctypes.c_int(0), ctypes.c_float(0.0)
+    cand_ms = (ctypes.c_float * nca)()
+    lib = N.load()
+    N.check(lib.sdemc_batch_autotune(N.ptr(plan.h_blob), N.ptr(plan.d_blob), N.ptr(plan.scratch),
+                                     plan.scratch.numel(), N.ptr(plan.out), ctypes.cast(bts, ctypes.c_void_p),
+                                     ctypes.cast(sides, ctypes.c_void_p), nca,
+                                     ctypes.cast(streams, ctypes.c_void_p) if max_side else None, max_side,
+                                     int(repeats), ctypes.cast(cfgs, ctypes.c_void_p), ctypes.byref(n_side),
+                                     ctypes.byref(ms), ctypes.cast(cand_ms, ctypes.c_void_p),
+                                     N.stream_handle(plan.device)), "sdemc_batch_autotune")
+    bt = int(cfgs[0].block_threads)
+    il = [int(cfgs[j].interleave) for j in range(nc)]
+    plan.set_config(bt, n_side.value, il)
+    entry = {"choice": [bt, n_side.value, il], "ms": ms.value,
+             "tried": sorted([[float(cand_ms[c]), candidates[c][0], candidates[c][1]] for c in range(nca)])}
     if use_cache:
         cache[sig] = entry
         _store_cache(cache)

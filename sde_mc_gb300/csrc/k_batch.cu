@@ -426,3 +426,76 @@ extern "C" int sdemc_price_batch(const void* h_blob, const void* d_blob, void* d
   batch_reduce_kernel<<<(unsigned)H.total_groups, kGroup, 0, s>>>(R);
   return check_cuda(cudaGetLastError(), "batch_reduce_kernel launch");
 }
+
+// ------------------------------------------------------------- autotune ----
+// Times sdemc_price_batch with CUDA events on `stream` (the plan blob must
+// already be on the device): first every (block_threads, side streams)
+// candidate, then, class by class, two paths per lane, kept when the whole
+// batch gets more than 1% faster.  Best of `repeats` launches after one warm
+// launch per setting.  Leaves d_out holding the last launch's results.
+namespace sdemc {
+static int time_batch(const void* h_blob, const void* d_blob, void* d_scratch, size_t scratch_bytes, double* d_out,
+                      const sdemc_cfg* cfgs, void* const* side, int n_side, int repeats, cudaStream_t s,
+                      cudaEvent_t e0, cudaEvent_t e1, float* ms) {
+  int rc = sdemc_price_batch(h_blob, d_blob, d_scratch, scratch_bytes, d_out, cfgs, side, n_side, s);
+  if (rc) return rc;
+  float best = 3.4e38f;
+  for (int r = 0; r < repeats; ++r) {
+    if ((rc = check_cuda(cudaEventRecord(e0, s), "event record"))) return rc;
+    if ((rc = sdemc_price_batch(h_blob, d_blob, d_scratch, scratch_bytes, d_out, cfgs, side, n_side, s))) return rc;
+    if ((rc = check_cuda(cudaEventRecord(e1, s), "event record"))) return rc;
+    if ((rc = check_cuda(cudaEventSynchronize(e1), "event sync"))) return rc;
+    float t = 0.f;
+    if ((rc = check_cuda(cudaEventElapsedTime(&t, e0, e1), "elapsed time"))) return rc;
+    if (t < best) best = t;
+  }
+  *ms = best;
+  return SDEMC_OK;
+}
+}  // namespace sdemc
+
+extern "C" int sdemc_batch_autotune(const void* h_blob, const void* d_blob, void* d_scratch, size_t scratch_bytes,
+                                    double* d_out, const int32_t* h_block_threads, const int32_t* h_side_counts,
+                                    int n_cand, void* const* side_streams, int max_side, int repeats,
+                                    sdemc_cfg* h_cfgs, int* h_n_side, float* h_ms, float* h_cand_ms,
+                                    void* stream) {
+  if (!h_blob || !h_block_threads || !h_side_counts || n_cand < 1 || !h_cfgs || !h_n_side || !h_ms || repeats < 1)
+    return fail(SDEMC_EINVAL, "bad autotune arguments");
+  const sdemc_batch_header& H = *static_cast<const sdemc_batch_header*>(h_blob);
+  const int nc = H.n_class > 0 ? H.n_class : 1;
+  for (int c = 0; c < n_cand; ++c) {
+    if (h_side_counts[c] < 0 || h_side_counts[c] > max_side || (h_side_counts[c] > 0 && !side_streams))
+      return fail(SDEMC_EINVAL, "candidate %d wants %d side streams (%d given)", c, h_side_counts[c], max_side);
+    const int bt = h_block_threads[c];
+    if (bt < 0 || bt > 256 || bt % 32) return fail(SDEMC_EINVAL, "candidate %d: block_threads %d", c, bt);
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = check_cuda(cudaEventCreate(&e0), "event create");
+  if (!rc) rc = check_cuda(cudaEventCreate(&e1), "event create");
+  float best = 3.4e38f;
+  int best_c = 0;
+  for (int c = 0; c < n_cand && !rc; ++c) {
+    for (int k = 0; k < nc; ++k) h_cfgs[k] = sdemc_cfg{h_block_threads[c], 0, 1, 0, 0};
+    float t = 0.f;
+    rc = time_batch(h_blob, d_blob, d_scratch, scratch_bytes, d_out, h_cfgs, side_streams, h_side_counts[c],
+                    repeats, s, e0, e1, &t);
+    if (!rc && h_cand_ms) h_cand_ms[c] = t;
+    if (!rc && t < best) { best = t; best_c = c; }
+  }
+  for (int k = 0; k < nc; ++k) h_cfgs[k] = sdemc_cfg{h_block_threads[best_c], 0, 1, 0, 0};
+  for (int k = 0; k < H.n_class && !rc; ++k) {
+    h_cfgs[k].interleave = 2;
+    float t = 0.f;
+    rc = time_batch(h_blob, d_blob, d_scratch, scratch_bytes, d_out, h_cfgs, side_streams, h_side_counts[best_c],
+                    repeats, s, e0, e1, &t);
+    if (!rc && t < 0.99f * best) best = t;
+    else h_cfgs[k].interleave = 1;
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (rc) return rc;
+  *h_n_side = h_side_counts[best_c];
+  *h_ms = best;
+  return SDEMC_OK;
+}
