@@ -114,56 +114,48 @@ SDEMC_DI void issue_rows(uint32_t d, uint32_t a, uint32_t lbo_a, uint32_t b, uin
 // Accumulator row -> ReLU -> BF16 into HH at column c0; mask bit f = (H_f > 0).
 SDEMC_DI void relu_to_hh(uint32_t ts, unsigned char* HH, int c0, uint32_t* mask) {
   mask[0] = mask[1] = 0u;
+  float v[kH];
+  tc::tmem_ld64(ts, v);
 #pragma unroll
-  for (int c = 0; c < kH / 16; ++c) {
-    float v[16];
-    tc::tmem_ld16(ts + 16 * c, v);
-    tc::tmem_ld_wait();
+  for (int j = 0; j < kH; ++j)
+    if (v[j] > 0.f) mask[j >> 5] |= 1u << (j & 31);
 #pragma unroll
-    for (int j = 0; j < 16; ++j)
-      if (v[j] > 0.f) mask[c >> 1] |= 1u << ((16 * c + j) & 31);
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      uint4 q;
-      q.x = tc::pack2(fmaxf(v[8 * h + 0], 0.f), fmaxf(v[8 * h + 1], 0.f));
-      q.y = tc::pack2(fmaxf(v[8 * h + 2], 0.f), fmaxf(v[8 * h + 3], 0.f));
-      q.z = tc::pack2(fmaxf(v[8 * h + 4], 0.f), fmaxf(v[8 * h + 5], 0.f));
-      q.w = tc::pack2(fmaxf(v[8 * h + 6], 0.f), fmaxf(v[8 * h + 7], 0.f));
-      *reinterpret_cast<uint4*>(HH + core_offset(threadIdx.x, c0 + 16 * c + 8 * h, kHW)) = q;
-    }
+  for (int c = 0; c < kH / 8; ++c) {
+    uint4 q;
+    q.x = tc::pack2(fmaxf(v[8 * c + 0], 0.f), fmaxf(v[8 * c + 1], 0.f));
+    q.y = tc::pack2(fmaxf(v[8 * c + 2], 0.f), fmaxf(v[8 * c + 3], 0.f));
+    q.z = tc::pack2(fmaxf(v[8 * c + 4], 0.f), fmaxf(v[8 * c + 5], 0.f));
+    q.w = tc::pack2(fmaxf(v[8 * c + 6], 0.f), fmaxf(v[8 * c + 7], 0.f));
+    *reinterpret_cast<uint4*>(HH + core_offset(threadIdx.x, c0 + 8 * c, kHW)) = q;
   }
 }
 
 // Masked accumulator row -> BF16 into DZ at column c0.
 SDEMC_DI void masked_to_dz(uint32_t ts, unsigned char* DZ, int c0, const uint32_t* mask) {
+  float v[kH];
+  tc::tmem_ld64(ts, v);
 #pragma unroll
-  for (int c = 0; c < kH / 16; ++c) {
-    float v[16];
-    tc::tmem_ld16(ts + 16 * c, v);
-    tc::tmem_ld_wait();
+  for (int j = 0; j < kH; ++j)
+    if (!((mask[j >> 5] >> (j & 31)) & 1u)) v[j] = 0.f;
 #pragma unroll
-    for (int j = 0; j < 16; ++j)
-      if (!((mask[c >> 1] >> ((16 * c + j) & 31)) & 1u)) v[j] = 0.f;
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      uint4 q;
-      q.x = tc::pack2(v[8 * h + 0], v[8 * h + 1]);
-      q.y = tc::pack2(v[8 * h + 2], v[8 * h + 3]);
-      q.z = tc::pack2(v[8 * h + 4], v[8 * h + 5]);
-      q.w = tc::pack2(v[8 * h + 6], v[8 * h + 7]);
-      *reinterpret_cast<uint4*>(DZ + core_offset(threadIdx.x, c0 + 16 * c + 8 * h, kDW)) = q;
-    }
+  for (int c = 0; c < kH / 8; ++c) {
+    uint4 q;
+    q.x = tc::pack2(v[8 * c + 0], v[8 * c + 1]);
+    q.y = tc::pack2(v[8 * c + 2], v[8 * c + 3]);
+    q.z = tc::pack2(v[8 * c + 4], v[8 * c + 5]);
+    q.w = tc::pack2(v[8 * c + 6], v[8 * c + 7]);
+    *reinterpret_cast<uint4*>(DZ + core_offset(threadIdx.x, c0 + 8 * c, kDW)) = q;
   }
 }
 
 // Masked accumulator row split into BF16 high and low parts: DZ columns
 // [0, 64) and [64, 128).
 SDEMC_DI void masked_split_to_dz(uint32_t ts, unsigned char* DZ, const uint32_t* mask) {
+  float vall[kH];
+  tc::tmem_ld64(ts, vall);
 #pragma unroll
   for (int c = 0; c < kH / 16; ++c) {
-    float v[16];
-    tc::tmem_ld16(ts + 16 * c, v);
-    tc::tmem_ld_wait();
+    const float* v = vall + 16 * c;
     __nv_bfloat16 hi[16], lo[16];
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
@@ -206,11 +198,11 @@ SDEMC_DI float reduce_scatter32(float* v) {
 // of chunk c holds W4[l >> 4][16 c + (l & 15)]).
 template <int D>
 SDEMC_DI void layer4_backward(BwdSmem& sm, uint32_t ts, const float* dO, float* acc4) {
+  float vall[kH];
+  tc::tmem_ld64(ts, vall);
 #pragma unroll
   for (int c = 0; c < kH / 16; ++c) {
-    float v[16];
-    tc::tmem_ld16(ts + 16 * c, v);
-    tc::tmem_ld_wait();
+    const float* v = vall + 16 * c;
     float dz[16], w[32];
 #pragma unroll
     for (int j = 0; j < 16; ++j) {

@@ -141,6 +141,21 @@ SDEMC_DI void tmem_ld16(uint32_t taddr, float* v) {
 }
 SDEMC_DI void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+// 64 consecutive FP32 columns of this thread's TMEM lane in one load; the
+// wait is in the same asm statement, so no use of the values can be
+// scheduled before the data has arrived.
+SDEMC_DI void tmem_ld64(uint32_t taddr, float* v) {
+  uint32_t r[64];
+  asm volatile(
+      "{\n tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32, %33, %34, %35, %36, %37, %38, %39, %40, %41, %42, %43, %44, %45, %46, %47, %48, %49, %50, %51, %52, %53, %54, %55, %56, %57, %58, %59, %60, %61, %62, %63}, [%64];\n"
+      " tcgen05.wait::ld.sync.aligned;\n}\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]), "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 64; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 SDEMC_DI uint32_t lane_base() { return (uint32_t)((threadIdx.x >> 5) * 32) << 16; }
 
 SDEMC_DI uint32_t pack2(float lo, float hi) {
@@ -272,20 +287,16 @@ SDEMC_DI bool product(TcSmem& sm, const unsigned char* A, const unsigned char* B
 // Accumulator row (bias included), ReLU, as the next A row (BF16).
 SDEMC_DI void relu_to_A(TcSmem& sm) {
   const uint32_t base = sm.tmem + lane_base();
+  float v[kH];
+  tmem_ld64(base, v);
 #pragma unroll
-  for (int c = 0; c < kH / 16; ++c) {
-    float v[16];
-    tmem_ld16(base + 16 * c, v);
-    tmem_ld_wait();
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      uint4 q;
-      q.x = pack2(fmaxf(v[8 * h + 0], 0.f), fmaxf(v[8 * h + 1], 0.f));
-      q.y = pack2(fmaxf(v[8 * h + 2], 0.f), fmaxf(v[8 * h + 3], 0.f));
-      q.z = pack2(fmaxf(v[8 * h + 4], 0.f), fmaxf(v[8 * h + 5], 0.f));
-      q.w = pack2(fmaxf(v[8 * h + 6], 0.f), fmaxf(v[8 * h + 7], 0.f));
-      *reinterpret_cast<uint4*>(sm.A + core_offset(threadIdx.x, 16 * c + 8 * h, kKH)) = q;
-    }
+  for (int c = 0; c < kH / 8; ++c) {
+    uint4 q;
+    q.x = pack2(fmaxf(v[8 * c + 0], 0.f), fmaxf(v[8 * c + 1], 0.f));
+    q.y = pack2(fmaxf(v[8 * c + 2], 0.f), fmaxf(v[8 * c + 3], 0.f));
+    q.z = pack2(fmaxf(v[8 * c + 4], 0.f), fmaxf(v[8 * c + 5], 0.f));
+    q.w = pack2(fmaxf(v[8 * c + 6], 0.f), fmaxf(v[8 * c + 7], 0.f));
+    *reinterpret_cast<uint4*>(sm.A + core_offset(threadIdx.x, 8 * c, kKH)) = q;
   }
 }
 
@@ -294,18 +305,14 @@ template <int D>
 SDEMC_DI void relu_layer4(TcSmem& sm, float* out) {
   const uint32_t base = sm.tmem + lane_base();
   float o0 = 0.f, o1 = 0.f;
+  float v[kH];
+  tmem_ld64(base, v);
 #pragma unroll
-  for (int c = 0; c < kH / 16; ++c) {
-    float v[16];
-    tmem_ld16(base + 16 * c, v);
-    tmem_ld_wait();
-#pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      const float h = fmaxf(v[j], 0.f);
-      const float2 w = sm.w4[16 * c + j];
-      o0 = __fmaf_rn(w.x, h, o0);
-      if (D > 1) o1 = __fmaf_rn(w.y, h, o1);
-    }
+  for (int j = 0; j < kH; ++j) {
+    const float h = fmaxf(v[j], 0.f);
+    const float2 w = sm.w4[j];
+    o0 = __fmaf_rn(w.x, h, o0);
+    if (D > 1) o1 = __fmaf_rn(w.y, h, o1);
   }
   out[0] = __fadd_rn(o0, sm.b4[0]);
   if (D > 1) out[1] = __fadd_rn(o1, sm.b4[1]);
