@@ -400,7 +400,6 @@ cv_backward_tc_kernel(const float* __restrict__ prm, const float* __restrict__ t
     for (int c = 0; c < 5; ++c) {
       float v[16];
       tc::tmem_ld16(tbase + kColW + c0 + 16 * c, v);
-      tc::tmem_ld_wait();
 #pragma unroll
       for (int jj = 0; jj < 16; ++jj) {
         const int i = 16 * c + jj;
@@ -410,7 +409,6 @@ cv_backward_tc_kernel(const float* __restrict__ prm, const float* __restrict__ t
     }
     float v1[16];
     tc::tmem_ld16(tbase + kColW1, v1);
-    tc::tmem_ld_wait();
     float g1[4];  // dW1[j][0..D], db1[j] of this row's part
 #pragma unroll
     for (int f = 0; f <= D; ++f) g1[f] = __fadd_rn(v1[3 * f], v1[3 * f + 1]);

@@ -126,12 +126,14 @@ SDEMC_DI void mma_commit(uint32_t mbar_saddr) {
                : "memory");
 }
 
-// 16 consecutive FP32 columns of this thread's TMEM lane.
+// 16 consecutive FP32 columns of this thread's TMEM lane; the wait for the
+// load is in the same asm statement, so no use of the values can be
+// scheduled before they have arrived.
 SDEMC_DI void tmem_ld16(uint32_t taddr, float* v) {
   uint32_t r[16];
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-      "%15}, [%16];"
+      "{\n tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];\n tcgen05.wait::ld.sync.aligned;\n}\n"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
         "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
       : "r"(taddr)
@@ -287,16 +289,19 @@ SDEMC_DI bool product(TcSmem& sm, const unsigned char* A, const unsigned char* B
 // Accumulator row (bias included), ReLU, as the next A row (BF16).
 SDEMC_DI void relu_to_A(TcSmem& sm) {
   const uint32_t base = sm.tmem + lane_base();
-  float v[kH];
-  tmem_ld64(base, v);
 #pragma unroll
-  for (int c = 0; c < kH / 8; ++c) {
-    uint4 q;
-    q.x = pack2(fmaxf(v[8 * c + 0], 0.f), fmaxf(v[8 * c + 1], 0.f));
-    q.y = pack2(fmaxf(v[8 * c + 2], 0.f), fmaxf(v[8 * c + 3], 0.f));
-    q.z = pack2(fmaxf(v[8 * c + 4], 0.f), fmaxf(v[8 * c + 5], 0.f));
-    q.w = pack2(fmaxf(v[8 * c + 6], 0.f), fmaxf(v[8 * c + 7], 0.f));
-    *reinterpret_cast<uint4*>(sm.A + core_offset(threadIdx.x, 8 * c, kKH)) = q;
+  for (int c = 0; c < kH / 16; ++c) {
+    float v[16];
+    tmem_ld16(base + 16 * c, v);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      uint4 q;
+      q.x = pack2(fmaxf(v[8 * h + 0], 0.f), fmaxf(v[8 * h + 1], 0.f));
+      q.y = pack2(fmaxf(v[8 * h + 2], 0.f), fmaxf(v[8 * h + 3], 0.f));
+      q.z = pack2(fmaxf(v[8 * h + 4], 0.f), fmaxf(v[8 * h + 5], 0.f));
+      q.w = pack2(fmaxf(v[8 * h + 6], 0.f), fmaxf(v[8 * h + 7], 0.f));
+      *reinterpret_cast<uint4*>(sm.A + core_offset(threadIdx.x, 16 * c + 8 * h, kKH)) = q;
+    }
   }
 }
 
@@ -305,14 +310,17 @@ template <int D>
 SDEMC_DI void relu_layer4(TcSmem& sm, float* out) {
   const uint32_t base = sm.tmem + lane_base();
   float o0 = 0.f, o1 = 0.f;
-  float v[kH];
-  tmem_ld64(base, v);
 #pragma unroll
-  for (int j = 0; j < kH; ++j) {
-    const float h = fmaxf(v[j], 0.f);
-    const float2 w = sm.w4[j];
-    o0 = __fmaf_rn(w.x, h, o0);
-    if (D > 1) o1 = __fmaf_rn(w.y, h, o1);
+  for (int c = 0; c < kH / 16; ++c) {
+    float v[16];
+    tmem_ld16(base + 16 * c, v);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      const float h = fmaxf(v[j], 0.f);
+      const float2 w = sm.w4[16 * c + j];
+      o0 = __fmaf_rn(w.x, h, o0);
+      if (D > 1) o1 = __fmaf_rn(w.y, h, o1);
+    }
   }
   out[0] = __fadd_rn(o0, sm.b4[0]);
   if (D > 1) out[1] = __fadd_rn(o1, sm.b4[1]);
