@@ -141,7 +141,6 @@ SDEMC_DI void tmem_ld16(uint32_t taddr, float* v) {
 #pragma unroll
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
-SDEMC_DI void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // 64 consecutive FP32 columns of this thread's TMEM lane in one load; the
 // wait is in the same asm statement, so no use of the values can be
