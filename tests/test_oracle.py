@@ -282,3 +282,16 @@ def test_cv_with_jump_integrand_restatement(oracle_mod):
     for i in range(8):
         np.testing.assert_allclose(gf[i], fx["gradf_%d" % i], rtol=2e-3, atol=1e-6)
         np.testing.assert_allclose(gg[i], fx["gradg_%d" % i], rtol=2e-3, atol=1e-6)
+
+
+def test_heston_closed_form_limits(oracle_mod):
+    """The Fourier-inversion Heston call (the independent check of the Heston
+    kernels) reduces to Black-Scholes when the variance is constant (v0 =
+    theta, vol of vol -> 0), decreases in the strike and stays inside the
+    no-arbitrage bounds."""
+    bs = oracle_mod.bs_call(1.0, 1.0, 1.0, 0.02, 0.2)
+    assert oracle_mod.heston_call(1.0, 0.04, 1.0, 1.0, 0.02, 2.0, 0.04, 1e-4, -0.7) == pytest.approx(bs, rel=1e-6)
+    prices = [oracle_mod.heston_call(1.0, 0.04, k, 1.0, 0.02, 2.0, 0.04, 0.3, -0.7) for k in (0.8, 0.9, 1.0, 1.1)]
+    assert all(a > b for a, b in zip(prices, prices[1:]))
+    for k, c in zip((0.8, 0.9, 1.0, 1.1), prices):
+        assert max(0.0, 1.0 - k * math.exp(-0.02)) < c < 1.0
