@@ -364,6 +364,9 @@ def bench_rainbow_plain(dev, steps, warmup, fp32_peak, mufu_peak):
                          "traffic": traffic["dram_bytes"] if traffic else None,
                          "traffic_note": "DRAM bytes of one ncu-captured launch (2^20 paths): descriptor and "
                                          "chunk partials only; paths stay in registers",
+                         "issue_active_ncu": traffic.get("issue_active") if traffic else None,
+                         "issue_note": "share of cycles an instruction issued (ncu, profiles/): the path loop is "
+                                       "issue-bound, mostly Philox's integer rounds, which count as no flop",
                          "kernel": "price_kernel<2,diag>", "kernel_ms": kernel_s * 1e3,
                          "flops_per_path_step": algorithmic_flops_per_path_step(2),
                          "peak_source": "measured FFMA probe on this GPU (sdemc_fp32_probe)",
@@ -859,6 +862,9 @@ def main():
                                  .get("serve_kernel<6,0,0,1>") or {}).get("dram_bytes"),
                      "traffic_note": "DRAM bytes of one ncu-captured serve_kernel launch (d = 6 main run): slot "
                                      "state and chunk partials only; paths stay in registers",
+                     "issue_active_ncu": ((load_json_file(os.path.join("profiles", "kernel_traffic.json")) or {})
+                                          .get("serve_kernel<6,0,0,1>") or {}).get("issue_active"),
+                     "issue_note": "share of cycles an instruction issued (ncu, profiles/)",
                      "kernel": "serve_kernel (all classes) over the server's device busy time",
                      "flops": "sum over requests of (pilot + main paths) x (steps + jump rate x T) x F(d)",
                      "peak_source": "measured FFMA probe on this GPU (sdemc_fp32_probe)",
