@@ -9,7 +9,7 @@
 // its path's control variate in 32-step ranges, exactly as K5 on tcgen05 sums
 // a materialised path, so Gamma matches that kernel bit for bit.  A 32-path
 // chunk stores (sum Gamma, sum Gamma^2, n, sum P, sum P^2) in FP64 — the plain
-// estimator stays alongside as the fallback and the judge of the control
+// estimator stays alongside as the fallback and the yardstick of the control
 // variate — and K10 sums the chunks in a fixed order.
 #include "mlp_tc.cuh"
 #include "sdemc_host.cuh"
