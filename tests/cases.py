@@ -52,6 +52,18 @@ def asian_merton(steps=20, seed=1):
             sm.ConstantShortRate(0.02))
 
 
+def loggbm_uniform(steps=16, seed=1):
+    """Log-price GBM (constant coefficients), call through Option.log."""
+    lg = sm.LogGbm(0.02, 0.25, torch.tensor([0.0]))
+    return sm.EulerSolver(lg, 1.0, steps, seed=seed), sm.EuroCall(1.0, log=True), sm.ConstantShortRate(0.02)
+
+
+def doublegbm_uniform(steps=12, seed=1):
+    """GBM driven by two independent 2-D Brownian motions ('indep')."""
+    dg = sm.DoubleGbm(0.03, torch.tensor([0.15, 0.2]), torch.tensor([0.1, 0.05]), torch.tensor([1.0, 1.2]), 2)
+    return sm.EulerSolver(dg, 1.0, steps, seed=seed), sm.Basket(1.0), sm.ConstantShortRate(0.02)
+
+
 def basket(d, steps=64, seed=1):
     rho = 0.3
     corr = sm.get_corr_matrix([rho] * (d * (d - 1) // 2)) if d > 1 else None
@@ -74,6 +86,8 @@ FIXTURE_CASES = {
     "replay_gbm_uniform": lambda: gbm_uniform(12),
     "replay_heston": lambda: heston(24),
     "replay_asian_merton": lambda: asian_merton(20),
+    "replay_loggbm_uniform": lambda: loggbm_uniform(16),
+    "replay_doublegbm_uniform": lambda: doublegbm_uniform(12),
 }
 
 

@@ -214,6 +214,35 @@ def cv_jump_fixture(sm, torch):
     np.savez_compressed(os.path.join(HERE, 'cv_mlp_jumps.npz'), **out)
 
 
+def uniform_replay(sm, torch, sol, bs, seed, payoff, csr):
+    """DiffusionSolver.solve (sde_mc/solvers.py:68-88) with every scheme call's
+    increments recorded."""
+    torch.manual_seed(seed)
+    rec = Recorder(sol)
+    paths, _ = sol.solve(bs=bs)
+    rec.restore()
+    return dict(bs=np.int64(bs), S=np.int64(sol.num_steps),
+                dw=torch.stack([cn for _, cn in rec.steps], 1).numpy().astype(np.float32),
+                paths=paths.numpy().astype(np.float32), chol=sol.lower_cholesky.numpy().astype(np.float32),
+                payoffs=(payoff(paths[:, -1]) * csr(sol.time_interval)).numpy().astype(np.float32))
+
+
+def diffusion_fixtures(sm, torch):
+    """Replay cases for the log-price GBM (sde_mc/sde.py:210-219, constant
+    coefficients, payoff through Option.log) and the two-Brownian 'indep'
+    GBM (sde.py:222-255, EulerScheme's summed diffusion, schemes.py:9-10)."""
+    csr = sm.ConstantShortRate(0.02)
+    cases = {}
+    lg = sm.LogGbm(0.02, 0.25, torch.tensor([0.0]))
+    cases['replay_loggbm_uniform'] = uniform_replay(sm, torch, sm.EulerSolver(lg, 1.0, 16), 24, 41,
+                                                    sm.EuroCall(1.0, log=True), csr)
+    dg = sm.DoubleGbm(0.03, torch.tensor([0.15, 0.2]), torch.tensor([0.1, 0.05]), torch.tensor([1.0, 1.2]), 2)
+    cases['replay_doublegbm_uniform'] = uniform_replay(sm, torch, sm.EulerSolver(dg, 1.0, 12), 24, 42,
+                                                       sm.Basket(1.0), csr)
+    for name, arrs in cases.items():
+        np.savez_compressed(os.path.join(HERE, name + '.npz'), **{k: np.asarray(v) for k, v in arrs.items()})
+
+
 def heston_asian_fixtures(sm, torch):
     """Replay cases for the two non-affine models: Heston with its implicit
     variance step (sde_mc/schemes.py:16-22, sde.py:258-279) on the uniform
@@ -262,7 +291,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--ref', default='/root/reference')
     ap.add_argument('--skip-stats', action='store_true')
-    ap.add_argument('--only', choices=['cv_jumps', 'heston_asian'], default=None,
+    ap.add_argument('--only', choices=['cv_jumps', 'heston_asian', 'diffusions'], default=None,
                     help='write only these fixtures')
     args = ap.parse_args()
     sm = load_reference(args.ref)
@@ -275,8 +304,12 @@ def main():
     if args.only == 'heston_asian':
         heston_asian_fixtures(sm, torch)
         return
+    if args.only == 'diffusions':
+        diffusion_fixtures(sm, torch)
+        return
     cv_jump_fixture(sm, torch)
     heston_asian_fixtures(sm, torch)
+    diffusion_fixtures(sm, torch)
 
     # ------------------------------------------------------------ KATs ----
     kat = {}

@@ -57,7 +57,8 @@ def _replay(oracle_mod, name):
 
 
 @pytest.mark.parametrize("name", ["replay_merton1d", "replay_merton2d_corr", "replay_merton2d_exact",
-                                  "replay_indep2d", "replay_gbm_uniform", "replay_asian_merton"])
+                                  "replay_indep2d", "replay_gbm_uniform", "replay_asian_merton",
+                                  "replay_loggbm_uniform", "replay_doublegbm_uniform"])
 def test_replay_bit_exact_vs_reference(oracle_mod, name):
     """Recorded reference draws through the oracle's loop give the reference's
     paths, time grid, left limits, jump marks and payoffs bit for bit."""
