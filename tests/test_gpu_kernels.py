@@ -63,7 +63,11 @@ def test_replay_matches_reference(name, oracle_mod):
     ref = oracle_mod.replay(inst, fx["dw"], fx.get("jump_times") if inst.grid == 0 else None,
                             fx.get("marks") if inst.grid == 0 else None, fx.get("asset"))
     np.testing.assert_array_equal(paths, ref["paths"])
-    np.testing.assert_array_equal(np_(out["payoffs"]), ref["payoffs"])
+    if inst.payoff_log:
+        # Option.log: CUDA's expf and libm's expf may round the last bit apart
+        np.testing.assert_allclose(np_(out["payoffs"]), ref["payoffs"], rtol=1e-6, atol=0)
+    else:
+        np.testing.assert_array_equal(np_(out["payoffs"]), ref["payoffs"])
 
 
 @pytest.mark.parametrize("name,factory,levels", [("mlmc_merton1d", lambda: merton1d(4), (8, 4)),
