@@ -14,4 +14,5 @@ from .mc import *
 from .mlmc import *
 from .nets import *
 from .varred import *
+from .problem import *
 from . import torch_ops  # registers torch.ops.sdemc.*

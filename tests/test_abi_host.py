@@ -333,3 +333,25 @@ def test_descriptor_and_launch_validation_on_the_host():
     lv = inst_for(levy2d(8), num_paths=64)
     assert lib.sdemc_price_f64(ctypes.byref(lv), fake, 1 << 30, out, None) == N.EUNSUPPORTED
 
+
+
+def test_problem_presets_lower():
+    """The reference's problem presets (sde_mc/problem.py) build on this
+    package's classes and lower to descriptors (host only)."""
+    presets = [sm.BlackScholesEuroCall.default_params(8, "cpu"), sm.BlackScholesRainbow.default_params(8, "cpu"),
+               sm.HestonEuroCall.default_params(8, "cpu"), sm.MertonEuroCall.default_params(8, "cpu"),
+               sm.LevyRainbow.default_params(8, "cpu"), sm.LevyRainbowMLMC(1, 1, 0.5, 2, 0.02, 0.3, 0.2, 0.001, 2,
+                                                                            1, 1, 3, 8, "cpu"),
+               sm.LevyCall.default_params(8, "cpu"), sm.LevyBestOf.default_params(8, "cpu"),
+               sm.LevyCallOnMax.default_params(2, 8, "cpu"), sm.LevyCallOnMax.default_params(4, 8, "cpu")]
+    dims = [1, 3, 2, 1, 2, 2, 1, 4, 2, 4]
+    for prob, d in zip(presets, dims):
+        assert prob.dim() == d
+        inst = lower(prob.solver, prob.payoff, prob.discounter, num_paths=16)
+        assert inst.dim == d and inst.num_steps == 8
+    assert presets[2].solver.__class__.__name__ == "HestonSolver" and \
+        lower(presets[2].solver, presets[2].payoff, presets[2].discounter).model == N.MODEL_HESTON
+    assert presets[5].solver.exact_jumps
+    assert isinstance(sm.LevyCallOnMax.default_params(3, 8, "cpu"), str)
+    presets[0].set_steps(20)
+    assert presets[0].solver.num_steps == 20
