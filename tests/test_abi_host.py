@@ -355,3 +355,22 @@ def test_problem_presets_lower():
     assert isinstance(sm.LevyCallOnMax.default_params(3, 8, "cpu"), str)
     presets[0].set_steps(20)
     assert presets[0].solver.num_steps == 20
+
+
+def test_c_client_compiles_and_runs(tmp_path):
+    """include/sdemc.h is plain C: a C99 program fills a descriptor, sizes the
+    scratch, plans a batch and sees malformed calls refused, linked against the
+    library (no GPU involved)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lib = os.path.join(ROOT, "sde_mc_gb300", "lib")
+    exe = str(tmp_path / "abi_client")
+    src = os.path.join(ROOT, "tests", "c_client", "abi_client.c")
+    subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), src, "-o", exe,
+                    "-L", lib, "-lsdemc", "-Wl,-rpath," + lib], check=True)
+    out = subprocess.run([exe], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert "c abi client ok" in out.stdout
