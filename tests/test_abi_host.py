@@ -1,6 +1,7 @@
 """CPU-side checks: the C-ABI library loads and exports every declared symbol,
 the ctypes descriptor matches the C layout, and the host-side API (lowering,
 payoffs, helpers, closed forms) matches the reference's known answers."""
+import math
 import os
 import re
 
@@ -374,3 +375,26 @@ def test_c_client_compiles_and_runs(tmp_path):
     out = subprocess.run([exe], capture_output=True, text=True)
     assert out.returncode == 0, out.stdout + out.stderr
     assert "c abi client ok" in out.stdout
+
+
+def test_served_stream_law():
+    """The served stream: Poisson arrivals at 2,000/s (exponential gaps), the
+    basket-mix instance law, targets drawn from {1e-2, 3e-3, 1e-3}, request
+    i on RNG stream i; a window starting at t_begin is the same requests,
+    shifted (host only)."""
+    from sde_mc_gb300 import stream as S
+    reqs = S.make_stream(2000.0, 0.5, seed=1)
+    n = len(reqs)
+    assert abs(n - 1000) < 4 * math.sqrt(1000)
+    gaps = np.diff([r.t for r in reqs])
+    assert (gaps > 0).all() and abs(gaps.mean() * 2000.0 - 1.0) < 0.1
+    assert abs(np.std(gaps) / gaps.mean() - 1.0) < 0.15   # exponential: cv = 1
+    targets = [r.target for r in reqs]
+    assert set(targets) == {1e-2, 3e-3, 1e-3}
+    assert all(abs(targets.count(t) / n - 1 / 3) < 0.06 for t in (1e-2, 3e-3, 1e-3))
+    assert [r.inst.stream_id for r in reqs] == [r.idx for r in reqs]
+    assert {r.dim for r in reqs} == set(range(1, 9))
+    win = S.make_stream(2000.0, 0.5, seed=1, t_begin=0.25)
+    late = [r for r in reqs if r.t >= 0.25]
+    assert [r.idx for r in win] == [r.idx for r in late]
+    assert all(abs(a.t - (b.t - 0.25)) < 1e-12 for a, b in zip(win, late))
