@@ -105,6 +105,18 @@ class JumpDiffusionSolver(SdeSolver):
     def add_jumps(self, t, old_x, x, jumps):
         return x + self.sde.jumps(t, old_x, jumps)
 
+    # Host helpers kept for callers that draw by hand (sde_mc/solvers.py:143-148);
+    # the kernels draw the same laws from their own Philox streams.
+    def sample_jump_times(self, size):
+        """Jump times: cumulative sums along dim 1 of exponential gaps at the
+        total jump rate."""
+        rate = float(torch.as_tensor(self.sde.jump_rate()).sum())
+        return torch.empty(size, device=self.device).exponential_(rate).cumsum(dim=1)
+
+    def sample_one_jump(self, size):
+        """One mark per path, repeated over the dimensions: (size, dim)."""
+        return self.sde.sample_jumps([size, 1], self.device).repeat(1, self.sde.dim)
+
     def init_storage(self, bs, steps, low_storage=False):
         paths = torch.zeros(size=(bs, steps + 1, self.sde.dim), device=self.device)
         if low_storage:

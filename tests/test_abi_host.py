@@ -398,3 +398,18 @@ def test_served_stream_law():
     late = [r for r in reqs if r.t >= 0.25]
     assert [r.idx for r in win] == [r.idx for r in late]
     assert all(abs(a.t - (b.t - 0.25)) < 1e-12 for a, b in zip(win, late))
+
+
+def test_jump_solver_host_samplers():
+    """sample_jump_times / sample_one_jump (sde_mc/solvers.py:143-148) for
+    callers that draw by hand: increasing exponential-gap times at the total
+    rate, one mark per path repeated over the dimensions."""
+    torch.manual_seed(3)
+    m = sm.Merton(0.02, 0.2, 2.0, -0.1, 0.2, torch.tensor([1., 1.]), dim=2)
+    sol = sm.JumpEulerSolver(m, 1.0, 10)
+    jt = sol.sample_jump_times((20000, 4, 1))
+    assert jt.shape == (20000, 4, 1) and bool((jt[:, 1:] >= jt[:, :-1]).all())
+    assert float(jt[:, 0].mean()) == pytest.approx(0.5, rel=0.03)
+    j = sol.sample_one_jump(5000)
+    assert j.shape == (5000, 2) and bool((j[:, 0] == j[:, 1]).all())
+    assert float(torch.log1p(j[:, 0]).mean()) == pytest.approx(-0.1, abs=0.015)
