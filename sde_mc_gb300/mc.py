@@ -11,6 +11,8 @@ import time
 
 import numpy as np
 import torch
+from scipy.stats import poisson  # noqa: F401  (re-exported as in sde_mc)
+from torch.utils.data import DataLoader  # noqa: F401  (re-exported as in sde_mc)
 
 from . import _native as N
 from . import kernels as K

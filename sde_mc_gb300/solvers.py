@@ -51,6 +51,11 @@ class SdeSolver(ABC):
     def init_storage(self, bs, steps):
         pass
 
+    def step(self, t, x, h, corr_normals):
+        """One scheme step on a host batch (the scheme mixed into a concrete
+        solver provides it, as in sde_mc/solvers.py:48, 61, 137)."""
+        raise NotImplementedError("a solver's step comes from its scheme (EulerScheme, HestonScheme)")
+
     def sample_corr_normals(self, size, h, corr=True):
         """Host helper kept for API compatibility: L @ (randn(size) * sqrt(h))."""
         normals = torch.randn(size=size, device=self.device) * torch.sqrt(torch.as_tensor(h))

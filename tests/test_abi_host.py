@@ -413,3 +413,23 @@ def test_jump_solver_host_samplers():
     j = sol.sample_one_jump(5000)
     assert j.shape == (5000, 2) and bool((j[:, 0] == j[:, 1]).all())
     assert float(torch.log1p(j[:, 0]).mean()) == pytest.approx(-0.1, abs=0.015)
+
+
+def test_public_names_cover_the_reference():
+    """Every public name of sde_mc's package namespace (as listed when the
+    fixtures were recorded) exists here, and the solver classes carry the
+    reference's public methods."""
+    names = ["AdaptedPathData", "AsianCall", "AsianWrapper", "Basket", "BestOf", "BinaryAoN", "ConstantShortRate",
+             "ControlVariate", "DataLoader", "Digital", "DiffusionSolver", "DoubleGbm", "EulerScheme",
+             "EulerSolver", "EuroCall", "EuroPut", "ExampleLevy", "ExpExampleLevy", "Gbm", "Gru", "Heston",
+             "HestonRainbow", "HestonScheme", "HestonSolver", "InverseCdf", "JumpDiffusionSolver",
+             "JumpEulerSolver", "Levy", "Levy2d", "LevySde", "LogGbm", "Lstm", "MCStatistics", "Merton", "Mlp",
+             "NormalJumpsPathData", "NormalPathData", "Option", "Rainbow", "Sde", "SdeSolver", "ZeroFunction",
+             "bs_asian_call", "bs_binary_aon", "bs_call", "bs_digital_call", "get_corr_matrix", "get_jump_comp",
+             "mc_multilevel", "mc_simple", "merton_call", "partition", "poisson", "remove_steps", "run_mc",
+             "solve_quadratic", "get_optimal_trials", "mc_estimates", "Problem", "HestonEuroCall"]
+    missing = [n for n in names if not hasattr(sm, n)]
+    assert not missing, missing
+    for cls in (sm.SdeSolver, sm.DiffusionSolver, sm.JumpDiffusionSolver):
+        assert hasattr(cls, "step") and hasattr(cls, "sample_corr_normals")
+    assert hasattr(sm.JumpDiffusionSolver, "sample_jump_times") and hasattr(sm.JumpDiffusionSolver, "sample_one_jump")
