@@ -65,7 +65,8 @@ def test_replay_matches_reference(name, oracle_mod):
     np.testing.assert_array_equal(paths, ref["paths"])
     if inst.payoff_log:
         # Option.log: CUDA's expf and libm's expf may round the last bit apart
-        np.testing.assert_allclose(np_(out["payoffs"]), ref["payoffs"], rtol=1e-6, atol=0)
+        # (1.2e-7 at exp(x) ~ 1, which max(exp(x) - K, 0) keeps as an absolute error)
+        np.testing.assert_allclose(np_(out["payoffs"]), ref["payoffs"], rtol=1e-6, atol=1e-6)
     else:
         np.testing.assert_array_equal(np_(out["payoffs"]), ref["payoffs"])
 
