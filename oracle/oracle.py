@@ -1,8 +1,9 @@
 """CPU oracle for the sde_mc path-integration hot path.
 
 TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the
-cpu_baseline leg of bench.py may import this module, and only as the checker
-(or the timed CPU baseline) — the product package never imports it.
+cpu_baseline leg of bench.py may import this module, and only to check the
+kernels' results (or as the timed CPU baseline) — the product package never
+imports it.
 
 Contents (each restating the reference, piers-hinds/sde_mc):
   * ctypes access to the C restatement ``sdemc_oracle.c`` of the solver loops

@@ -2,8 +2,9 @@
  * sdemc_oracle.c — CPU oracle for the sde_mc path-integration hot path.
  *
  * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the
- * cpu_baseline leg of bench.py may load this library, and only as the
- * checker or as the timed CPU baseline — never as part of the product path.
+ * cpu_baseline leg of bench.py may load this library, and only to check the
+ * kernels' results or as the timed CPU baseline — never as part of the
+ * product path.
  *
  * A plain-C restatement of the reference's algorithm (piers-hinds/sde_mc):
  *   - the jump-adapted Euler loop of JumpDiffusionSolver.solve
