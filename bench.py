@@ -155,6 +155,12 @@ def algorithmic_flops_per_path_step(d):
     return 5 + 10 * d + (d * (d + 1) if d > 1 else 0)
 
 
+# one earlier measurement on a GB300 each (copy bandwidth; cuBLAS bf16 burst),
+# used only when MEASURED_PEAKS.json is absent
+HBM_FALLBACK_GBS = 6800.0
+BF16_FALLBACK_TFLOPS = 1900.0
+
+
 def load_json_file(name):
     p = os.path.join(ROOT, name)
     if os.path.exists(p):
@@ -377,7 +383,7 @@ def bench_rainbow_plain(dev, steps, warmup, fp32_peak, mufu_peak):
             "l2": "flushed (256 MB write) between timed steps", "gpu_launches": 2 * steps}
 
 
-def bench_materialise(dev, hbm_peak):
+def bench_materialise(dev, hbm_peak, peak_source="MEASURED_PEAKS.json hbm_gbs (copy, read + write)"):
     """Materialised mode (K4): the 2D rainbow's paths in the AdaptedPathData
     layout (paths, left limits, time, jumps: S + 1 rows; normals: S rows),
     2^20 paths, timed on the kernel alone; HBM roofline of the stores."""
@@ -425,7 +431,7 @@ def bench_materialise(dev, hbm_peak):
             "bytes_written": nbytes, "ms": t * 1e3, "path_steps_per_s": executed / t,
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
                          "frac": gbs / hbm_peak if hbm_peak else None,
-                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy, read + write)",
+                         "peak_source": peak_source,
                          "bytes": "the layout's arrays: (S + 1) rows x (3d + 1) floats + S rows x d floats "
                                   "per path, + payoff and step count"},
             "l2": "outputs (%.1f GB) far larger than L2" % (nbytes / 1e9)}
@@ -560,6 +566,9 @@ def bench_cv_learned(dev, epochs=10):
     rows_eval = n_eval * eval_steps
     peaks = load_json_file("MEASURED_PEAKS.json") or {}
     bf16 = peaks.get("bf16_tflops")
+    bf16_source = "MEASURED_PEAKS.json bf16_tflops (cuBLAS burst)"
+    if not bf16:
+        bf16, bf16_source = BF16_FALLBACK_TFLOPS, "fallback 1.9 PFLOP/s (MEASURED_PEAKS.json absent)"
     tf_train = rows_train * 4 * fwd / t_train / 1e12
     tf_eval = rows_eval * fwd / t_eval / 1e12
     # the served form's regression control variate on the same model and target
@@ -576,7 +585,7 @@ def bench_cv_learned(dev, epochs=10):
             "loss_first_last": [losses[0], losses[-1]], "simulate_s": t_sim, "train_s": t_train, "eval_s": t_eval,
             "train_rows": rows_train, "eval_rows": rows_eval,
             "train_tflops": tf_train, "eval_tflops_incl_paths": tf_eval,
-            "bf16_peak_tflops": bf16, "train_frac_of_bf16_peak": (tf_train / bf16) if bf16 else None,
+            "bf16_peak_tflops": bf16, "bf16_peak_source": bf16_source, "train_frac_of_bf16_peak": tf_train / bf16,
             "regression_cv_same_model": {"vrf": reg[2].vrf, "mean": reg[2].mean, "se": reg[2].se,
                                          "plain_mean": reg[1].mean, "plain_se": reg[1].se,
                                          "main_paths_cv": reg[2].main_paths, "main_paths_plain": reg[1].main_paths},
@@ -885,7 +894,11 @@ def main():
             line["rainbow2d_plain"] = _section(bench_rainbow_plain, dev, 20, 5, fp32_peak, mufu_peak)
         if "materialise" in secs:
             peaks = load_json_file("MEASURED_PEAKS.json") or {}
-            line["materialised_mode"] = _section(bench_materialise, dev, peaks.get("hbm_gbs"))
+            if peaks.get("hbm_gbs"):
+                line["materialised_mode"] = _section(bench_materialise, dev, peaks["hbm_gbs"])
+            else:
+                line["materialised_mode"] = _section(bench_materialise, dev, HBM_FALLBACK_GBS,
+                                                     "fallback 6.8 TB/s (MEASURED_PEAKS.json absent)")
         if "mlmc" in secs:
             line["rainbow2d_mlmc"] = _section(bench_rainbow_mlmc, dev)
         if "mix" in secs:
