@@ -20,8 +20,7 @@ import sde_mc_gb300 as sm
 from tests.cases import basket, indep2d, inst_for, levy2d, merton1d, zdim
 
 
-def _normals(inst, paths, steps):
-    from oracle import oracle as O
+def _normals(O, inst, paths, steps):
     return np.stack([O.native_normals(inst, p, steps, zdim(inst)) for p in range(paths)])
 
 
@@ -29,8 +28,8 @@ def _normals(inst, paths, steps):
                                                  (lambda: indep2d(64), 1500, 64),
                                                  (lambda: basket(5, 32), 1000, 32),
                                                  (lambda: basket(8, 16), 1000, 16)])
-def test_normals_are_independent_standard_normals(factory, paths, steps):
-    z = _normals(inst_for(factory(), seed=11), paths, steps).astype(np.float64)  # (paths, steps, ZD)
+def test_normals_are_independent_standard_normals(factory, paths, steps, oracle_mod):
+    z = _normals(oracle_mod, inst_for(factory(), seed=11), paths, steps).astype(np.float64)  # (paths, steps, ZD)
     n = z.size
     assert abs(z.mean()) < 5 / np.sqrt(n)
     assert abs(z.var() - 1.0) < 5 * np.sqrt(2.0 / n)
@@ -47,8 +46,8 @@ def test_normals_are_independent_standard_normals(factory, paths, steps):
     assert abs(np.mean(z[1:] * z[:-1])) < 5 / np.sqrt((paths - 1) * steps * z.shape[2])
 
 
-def test_different_seeds_streams_and_paths_give_different_draws():
-    from oracle import oracle as O
+def test_different_seeds_streams_and_paths_give_different_draws(oracle_mod):
+    O = oracle_mod
     a = inst_for(merton1d(16), seed=1)
     b = inst_for(merton1d(16), seed=2)
     za, zb = O.native_normals(a, 0, 16, 1), O.native_normals(b, 0, 16, 1)
@@ -62,8 +61,7 @@ def test_different_seeds_streams_and_paths_give_different_draws():
     np.testing.assert_array_equal(O.native_normals(a, 9, 16, 1), O.native_normals(c, 2, 16, 1))
 
 
-def _jumps(inst, paths, n):
-    from oracle import oracle as O
+def _jumps(O, inst, paths, n):
     out = [O.native_jumps(inst, p, n) for p in range(paths)]
     jt = np.stack([o[0] for o in out]).astype(np.float64)
     jm = np.stack([o[1] for o in out]).astype(np.float64)
@@ -71,9 +69,9 @@ def _jumps(inst, paths, n):
     return jt, jm, js
 
 
-def test_merton_gaps_and_marks():
+def test_merton_gaps_and_marks(oracle_mod):
     inst = inst_for(merton1d(16), seed=3)
-    jt, jm, _ = _jumps(inst, 2000, 8)
+    jt, jm, _ = _jumps(oracle_mod, inst, 2000, 8)
     gaps = np.diff(np.concatenate([np.zeros((jt.shape[0], 1)), jt], 1), axis=1).ravel()
     rate = float(inst.rate)
     assert rate == pytest.approx(2.0)
@@ -86,10 +84,10 @@ def test_merton_gaps_and_marks():
     assert abs(np.corrcoef(gaps, logj)[0, 1]) < 5 / np.sqrt(gaps.size)
 
 
-def test_per_asset_jumps_pick_assets_by_rate():
+def test_per_asset_jumps_pick_assets_by_rate(oracle_mod):
     case = indep2d(16)
     inst = inst_for(case, seed=4)
-    jt, jm, js = _jumps(inst, 2000, 8)
+    jt, jm, js = _jumps(oracle_mod, inst, 2000, 8)
     # IndependentJumpsMerton with rates (1, 1): total rate 2, each asset half the jumps
     assert float(inst.rate) == pytest.approx(2.0)
     counts = np.bincount(js.ravel(), minlength=2)
@@ -102,15 +100,15 @@ def test_per_asset_jumps_pick_assets_by_rate():
     m = sm.IndependentJumpsMerton(0.02, torch.tensor([0.2, 0.3, 0.25]), [0.5, 1.0, 2.5], -0.05, 0.15,
                                   torch.ones(3), 3)
     inst3 = inst_for((sm.JumpEulerSolver(m, 1.0, 16), sm.Rainbow(1.0), sm.ConstantShortRate(0.02)), seed=5)
-    _, _, js3 = _jumps(inst3, 2000, 8)
+    _, _, js3 = _jumps(oracle_mod, inst3, 2000, 8)
     counts = np.bincount(js3.ravel(), minlength=3)
     assert stats.chisquare(counts, js3.size * np.array([0.5, 1.0, 2.5]) / 4.0).pvalue > 1e-4
 
 
-def test_levy_marks_follow_the_truncated_jump_measure():
+def test_levy_marks_follow_the_truncated_jump_measure(oracle_mod):
     solver, _, _ = levy2d(16)
     inst = inst_for((solver, sm.Rainbow(1.0), sm.ConstantShortRate(0.02)), seed=6)
-    _, jm, _ = _jumps(inst, 2000, 8)
+    _, jm, _ = _jumps(oracle_mod, inst, 2000, 8)
     x = jm.ravel()
     ic = solver.sde.levy.icdf
     assert np.all(np.abs(x) >= ic.eps * (1 - 1e-5))
