@@ -189,6 +189,11 @@ int sdemc_fp32_probe(int iters, float* d_sink, int sink_len, double* h_flops,
  * operations of the launch.                                                */
 int sdemc_mufu_probe(int iters, float* d_sink, int sink_len, double* h_ops,
                      void* stream);
+/* The give-up path of the tensor-core kernels' bounded mbarrier waits: one
+ * warp waits, through the same wait, on a barrier that nothing arrives at and
+ * gives up after `spins` polls (1 .. 2^22), OR-ing SDEMC_ETIMEOUT into
+ * *d_status; the context stays usable.  For tests of the failure path.     */
+int sdemc_wait_probe(int spins, int32_t* d_status, void* stream);
 
 /* ---- K1: fused pricing ------------------------------------------------
  * Replaces mc_simple (sde_mc/mc.py:53-123) over JumpDiffusionSolver.solve

@@ -116,6 +116,7 @@ _PROTOS = {
                           ctypes.c_uint32, _I, _P, _P]),
     "sdemc_fp32_probe": (_I, [_I, _P, _I, ctypes.POINTER(ctypes.c_double), _P]),
     "sdemc_mufu_probe": (_I, [_I, _P, _I, ctypes.POINTER(ctypes.c_double), _P]),
+    "sdemc_wait_probe": (_I, [_I, _P, _P]),
 }
 EXPORTED = tuple(_PROTOS)
 

@@ -133,6 +133,27 @@ static int launch_tc(const float* prm, const float* time, const float* paths, co
 
 using namespace sdemc;
 
+// The give-up path of the bounded waits: one warp waits, through the same
+// tc::mbar_wait the tensor-core kernels use, on an mbarrier that nothing
+// arrives at, and records SDEMC_ETIMEOUT when the wait returns false.
+__global__ void wait_probe_kernel(int spins, int32_t* status) {
+  __shared__ uint64_t bar;
+  const uint32_t a = tc::saddr_of(&bar);
+  if (threadIdx.x == 0) {
+    tc::mbar_init(a);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const bool ok = tc::mbar_wait(a, 0u, spins);
+  if (!ok && threadIdx.x == 0) atomicOr(status, SDEMC_ETIMEOUT);
+}
+
+extern "C" int sdemc_wait_probe(int spins, int32_t* d_status, void* stream) {
+  if (spins < 1 || spins > tc::kMaxSpins || !d_status) return fail(SDEMC_EINVAL, "bad wait_probe arguments");
+  wait_probe_kernel<<<1, 32, 0, (cudaStream_t)stream>>>(spins, d_status);
+  return check_cuda(cudaGetLastError(), "wait_probe launch");
+}
+
 extern "C" size_t sdemc_cv_forward_tc_scratch_bytes(int64_t n, int steps) {
   if (n < 1 || steps < 1) return 0;
   int nr = 1, len = 1;

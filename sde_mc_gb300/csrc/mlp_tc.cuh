@@ -92,9 +92,10 @@ SDEMC_DI void mbar_init(uint32_t addr) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(addr) : "memory");
 }
 
-// Bounded wait for the phase with the given parity to complete.
-SDEMC_DI bool mbar_wait(uint32_t addr, uint32_t parity) {
-  for (int it = 0; it < kMaxSpins; ++it) {
+// Bounded wait for the phase with the given parity to complete; false after
+// `limit` polls.
+SDEMC_DI bool mbar_wait(uint32_t addr, uint32_t parity, int limit = kMaxSpins) {
+  for (int it = 0; it < limit; ++it) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"

@@ -333,6 +333,10 @@ def test_descriptor_and_launch_validation_on_the_host():
     assert lib.sdemc_price_f64(ctypes.byref(f), fake, 0, out, None) == N.ENOMEM
     lv = inst_for(levy2d(8), num_paths=64)
     assert lib.sdemc_price_f64(ctypes.byref(lv), fake, 1 << 30, out, None) == N.EUNSUPPORTED
+    # the wait probe's poll limit is the kernels' own bound, 1 .. 2^22
+    assert lib.sdemc_wait_probe(0, fake, None) == N.EINVAL
+    assert lib.sdemc_wait_probe((1 << 22) + 1, fake, None) == N.EINVAL
+    assert lib.sdemc_wait_probe(16, None, None) == N.EINVAL
 
 
 

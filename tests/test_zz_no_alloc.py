@@ -3,8 +3,8 @@
 Hosts that own all GPU memory through their own pool, or that must not call
 cudaMalloc while building a CUDA graph, call this entry point with only their
 inputs and outputs; its scratch is a fixed array inside the library.  This file
-is collected last so that a run stopping at the first failure has already run
-every other test; it also passes on its own in a fresh process.
+is collected after the other kernel tests, so that a run stopping at the first
+failure has already run them; it also passes on its own in a fresh process.
 """
 import ctypes
 
