@@ -243,6 +243,20 @@ def diffusion_fixtures(sm, torch):
         np.savez_compressed(os.path.join(HERE, name + '.npz'), **{k: np.asarray(v) for k, v in arrs.items()})
 
 
+def levy_mlmc_fixture(sm, torch):
+    """The MLMC coupling of the Levy rainbow preset (LevyRainbowMLMC,
+    sde_mc/problem.py:93-106): the 2-D ExpExampleLevy 'indep' model on the
+    jump-adapted grid with exact_jumps=True (the jump reads the post-diffusion
+    state), through JumpDiffusionSolver.multilevel_solve
+    (sde_mc/solvers.py:228-307) with factor 2."""
+    lev = sm.ExpExampleLevy(1, 1, 0.5, 2, 0.02, 0.2, 0.2, 0.2, 2)
+    lsde = sm.LevySde(lev, torch.ones(2))
+    sol = sm.JumpEulerSolver(lsde, 1.0, 4, exact_jumps=True)
+    c = mlmc_replay_case(sm, torch, sol, 32, (8, 4), seed=19)
+    c.update(max_jumps=np.int64(sol.max_jumps), exact_jumps=np.int64(1))
+    np.savez_compressed(os.path.join(HERE, 'mlmc_levy2d_exact.npz'), **{k: np.asarray(v) for k, v in c.items()})
+
+
 def heston_asian_fixtures(sm, torch):
     """Replay cases for the two non-affine models: Heston with its implicit
     variance step (sde_mc/schemes.py:16-22, sde.py:258-279) on the uniform
@@ -291,7 +305,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--ref', default='/root/reference')
     ap.add_argument('--skip-stats', action='store_true')
-    ap.add_argument('--only', choices=['cv_jumps', 'heston_asian', 'diffusions'], default=None,
+    ap.add_argument('--only', choices=['cv_jumps', 'heston_asian', 'diffusions', 'levy_mlmc'], default=None,
                     help='write only these fixtures')
     args = ap.parse_args()
     sm = load_reference(args.ref)
@@ -307,9 +321,13 @@ def main():
     if args.only == 'diffusions':
         diffusion_fixtures(sm, torch)
         return
+    if args.only == 'levy_mlmc':
+        levy_mlmc_fixture(sm, torch)
+        return
     cv_jump_fixture(sm, torch)
     heston_asian_fixtures(sm, torch)
     diffusion_fixtures(sm, torch)
+    levy_mlmc_fixture(sm, torch)
 
     # ------------------------------------------------------------ KATs ----
     kat = {}

@@ -4,7 +4,9 @@ import math
 
 import numpy as np
 import pytest
+import torch
 
+import sde_mc_gb300 as sm
 from tests.cases import FIXTURE_CASES, inst_for, merton1d, indep2d
 from tests.conftest import load_npz
 
@@ -168,6 +170,24 @@ def test_mlmc_replay_bit_exact(oracle_mod, name, factory, levels):
     assert out["rc"] == 0
     np.testing.assert_array_equal(out["xf"], fx["xf"])
     np.testing.assert_array_equal(out["xc"], fx["xc"])
+
+
+def test_mlmc_replay_levy_exact_jumps(oracle_mod):
+    """The LevyRainbowMLMC coupling (sde_mc/problem.py:93-106): 2-D Levy
+    'indep' model, exact_jumps=True, factor 2.  Within 1e-5 as the Levy
+    replay (the drift folds -f*gamma into one coefficient); most paths are
+    bit-exact."""
+    fx = load_npz("mlmc_levy2d_exact")
+    lev = sm.ExpExampleLevy(1, 1, 0.5, 2, 0.02, 0.2, 0.2, 0.2, 2)
+    solver = sm.JumpEulerSolver(sm.LevySde(lev, torch.ones(2)), 1.0, 4, exact_jumps=True)
+    inst = inst_for((solver, sm.Rainbow(1.0), sm.ConstantShortRate(0.02)), num_paths=int(fx["bs"]), steps=4)
+    assert inst.exact_jumps == 1 and int(fx["max_jumps"]) == solver.max_jumps
+    out = oracle_mod.mlmc_replay(inst, 2, float(fx["h_fine"]), float(fx["h_coarse"]), fx["dw"],
+                                 fx["marks"].shape[1], fx["jump_times"], fx["marks"])
+    assert out["rc"] == 0
+    for k in ("xf", "xc"):
+        np.testing.assert_allclose(out[k], fx[k], rtol=1e-5, atol=1e-6)
+        assert np.mean(np.all(out[k] == fx[k], axis=1)) > 0.8
 
 
 @pytest.mark.parametrize("name,levels,exact", [("mlmc_heston", (8, 4), False), ("mlmc_heston_f4", (16, 4), True)])
