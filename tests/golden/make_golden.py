@@ -244,17 +244,23 @@ def diffusion_fixtures(sm, torch):
 
 
 def levy_mlmc_fixture(sm, torch):
-    """The MLMC coupling of the Levy rainbow preset (LevyRainbowMLMC,
-    sde_mc/problem.py:93-106): the 2-D ExpExampleLevy 'indep' model on the
-    jump-adapted grid with exact_jumps=True (the jump reads the post-diffusion
-    state), through JumpDiffusionSolver.multilevel_solve
-    (sde_mc/solvers.py:228-307) with factor 2."""
+    """MLMC couplings beyond Merton, through JumpDiffusionSolver.multilevel_solve
+    (sde_mc/solvers.py:228-307) with factor 2: the Levy rainbow preset's
+    (LevyRainbowMLMC, sde_mc/problem.py:93-106; the 2-D ExpExampleLevy 'indep'
+    model with exact_jumps=True, the jump reading the post-diffusion state)
+    and the Asian wrapper's around a 1-D Merton."""
     lev = sm.ExpExampleLevy(1, 1, 0.5, 2, 0.02, 0.2, 0.2, 0.2, 2)
     lsde = sm.LevySde(lev, torch.ones(2))
     sol = sm.JumpEulerSolver(lsde, 1.0, 4, exact_jumps=True)
     c = mlmc_replay_case(sm, torch, sol, 32, (8, 4), seed=19)
     c.update(max_jumps=np.int64(sol.max_jumps), exact_jumps=np.int64(1))
     np.savez_compressed(os.path.join(HERE, 'mlmc_levy2d_exact.npz'), **{k: np.asarray(v) for k, v in c.items()})
+    # AsianWrapper (sde_mc/sde.py:378-406) around a 1-D Merton, same coupling
+    m = sm.Merton(0.02, 0.2, 2.0, -0.1, 0.2, torch.tensor([1.]), dim=1)
+    sol = sm.JumpEulerSolver(sm.AsianWrapper(m), 1.0, 4)
+    c = mlmc_replay_case(sm, torch, sol, 32, (8, 4), seed=20)
+    c.update(max_jumps=np.int64(sol.max_jumps), exact_jumps=np.int64(0))
+    np.savez_compressed(os.path.join(HERE, 'mlmc_asian_merton.npz'), **{k: np.asarray(v) for k, v in c.items()})
 
 
 def heston_asian_fixtures(sm, torch):

@@ -7,7 +7,7 @@ import pytest
 import torch
 
 import sde_mc_gb300 as sm
-from tests.cases import FIXTURE_CASES, inst_for, merton1d, indep2d
+from tests.cases import FIXTURE_CASES, asian_merton, indep2d, inst_for, merton1d
 from tests.conftest import load_npz
 
 
@@ -161,7 +161,8 @@ def test_replay_levy_within_tolerance(oracle_mod):
 
 
 @pytest.mark.parametrize("name,factory,levels", [("mlmc_merton1d", lambda: merton1d(4), (8, 4)),
-                                                 ("mlmc_indep2d", lambda: indep2d(8), (16, 8))])
+                                                 ("mlmc_indep2d", lambda: indep2d(8), (16, 8)),
+                                                 ("mlmc_asian_merton", lambda: asian_merton(4), (8, 4))])
 def test_mlmc_replay_bit_exact(oracle_mod, name, factory, levels):
     fx = load_npz(name)
     inst = inst_for(factory(), num_paths=int(fx["bs"]), steps=levels[1])
