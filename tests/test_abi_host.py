@@ -31,6 +31,22 @@ def test_library_exports_every_declared_symbol():
     assert set(decl) == set(N.EXPORTED)
 
 
+def test_library_exports_nothing_undeclared():
+    """The shared library's dynamic symbol table holds the header's entry
+    points and no other public name (the CUDA runtime is linked statically
+    and stays hidden)."""
+    import shutil
+    import subprocess
+    nm = shutil.which("nm")
+    if nm is None:
+        pytest.skip("nm not available")
+    N.load()
+    out = subprocess.run([nm, "-D", "--defined-only", N.LIB_PATH], capture_output=True, text=True, check=True)
+    names = {ln.split()[-1] for ln in out.stdout.splitlines() if ln.strip()}
+    public = {n for n in names if not n.startswith("_")}
+    assert public == set(declared_symbols()), sorted(public ^ set(declared_symbols()))
+
+
 def test_descriptor_layout_matches_header():
     lib = N.load()
     assert lib.sdemc_abi_version() == 1
