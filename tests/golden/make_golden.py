@@ -263,6 +263,34 @@ def levy_mlmc_fixture(sm, torch):
     np.savez_compressed(os.path.join(HERE, 'mlmc_asian_merton.npz'), **{k: np.asarray(v) for k, v in c.items()})
 
 
+def model_stats(sm, torch):
+    """The reference's own plain estimates (mc_simple, sde_mc/mc.py:53-123)
+    for the model kinds beyond Merton: Heston (HestonSolver), the Asian
+    wrapper around a 1-D Merton, the 2-D Levy rainbow and the log-price GBM
+    with its payoff through Option.log.  Added to stats.json."""
+    path = os.path.join(HERE, 'stats.json')
+    with open(path) as fh:
+        stats = json.load(fh)
+    csr = sm.ConstantShortRate(0.02)
+    runs = {}
+    h = sm.Heston(0.02, 2.0, 0.04, 0.3, -0.7, torch.tensor([1., 0.04]))
+    runs['heston_64_2p16'] = (sm.HestonSolver(h, 1.0, 64, seed=41), sm.EuroCall(1.0), 'terminal')
+    m = sm.Merton(0.02, 0.2, 2.0, -0.1, 0.2, torch.tensor([1.]), dim=1)
+    runs['asian_merton_20_2p16'] = (sm.JumpEulerSolver(sm.AsianWrapper(m), 1.0, 20, seed=42), sm.AsianCall(1.0, 1.0),
+                                    'adapted')
+    lev = sm.ExpExampleLevy(1, 1, 0.5, 2, 0.02, 0.2, 0.2, 0.2, 2)
+    runs['levy2d_16_2p16'] = (sm.JumpEulerSolver(sm.LevySde(lev, torch.ones(2)), 1.0, 16, seed=43), sm.Rainbow(1.0),
+                              'adapted')
+    lg = sm.LogGbm(0.02, 0.25, torch.tensor([0.0]))
+    runs['loggbm_16_2p16'] = (sm.EulerSolver(lg, 1.0, 16, seed=44), sm.EuroCall(1.0, log=True), 'terminal')
+    for name, (sol, pay, pt) in runs.items():
+        ts = time.time()
+        st = sm.mc_simple(2 ** 16, sol, pay, csr, bs=2 ** 14, payoff_time=pt)
+        stats[name] = dict(mean=float(st.sample_mean), se=float(st.sample_std), n=2 ** 16, seconds=time.time() - ts)
+    with open(path, 'w') as fh:
+        json.dump(stats, fh, indent=1, sort_keys=True)
+
+
 def heston_asian_fixtures(sm, torch):
     """Replay cases for the two non-affine models: Heston with its implicit
     variance step (sde_mc/schemes.py:16-22, sde.py:258-279) on the uniform
@@ -311,7 +339,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--ref', default='/root/reference')
     ap.add_argument('--skip-stats', action='store_true')
-    ap.add_argument('--only', choices=['cv_jumps', 'heston_asian', 'diffusions', 'levy_mlmc'], default=None,
+    ap.add_argument('--only', choices=['cv_jumps', 'heston_asian', 'diffusions', 'levy_mlmc', 'model_stats'],
+                    default=None,
                     help='write only these fixtures')
     args = ap.parse_args()
     sm = load_reference(args.ref)
@@ -329,6 +358,9 @@ def main():
         return
     if args.only == 'levy_mlmc':
         levy_mlmc_fixture(sm, torch)
+        return
+    if args.only == 'model_stats':
+        model_stats(sm, torch)
         return
     cv_jump_fixture(sm, torch)
     heston_asian_fixtures(sm, torch)
@@ -533,6 +565,7 @@ def main():
                                            oracle=float(sm.bs_call(1, 1, 1, 0.02, 0.2)))
         with open(os.path.join(HERE, 'stats.json'), 'w') as fh:
             json.dump(stats, fh, indent=1, sort_keys=True)
+        model_stats(sm, torch)
     print('golden fixtures written in %.1f s' % (time.time() - t0))
 
 

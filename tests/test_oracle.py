@@ -7,7 +7,7 @@ import pytest
 import torch
 
 import sde_mc_gb300 as sm
-from tests.cases import FIXTURE_CASES, asian_merton, indep2d, inst_for, merton1d
+from tests.cases import FIXTURE_CASES, asian_merton, heston, indep2d, inst_for, levy2d, loggbm_uniform, merton1d
 from tests.conftest import load_npz
 
 
@@ -275,6 +275,22 @@ def test_native_price_c2_vs_reference(oracle_mod, ref_stats):
     se = math.sqrt(out[4] / out[2])
     r = ref_stats["c2_plain_2p16"]
     assert abs(out[3] - r["mean"]) < 3 * math.hypot(se, r["se"])
+
+
+@pytest.mark.parametrize("name,factory", [("heston_64_2p16", lambda: heston(64)),
+                                          ("asian_merton_20_2p16", lambda: asian_merton(20)),
+                                          ("levy2d_16_2p16", lambda: levy2d(16)),
+                                          ("loggbm_16_2p16", lambda: loggbm_uniform(16))])
+def test_native_price_vs_reference_estimates(oracle_mod, ref_stats, name, factory):
+    """The oracle's own Philox run of each model kind against the reference's
+    mc_simple estimate of the same problem (independent draws): within 3
+    combined standard errors."""
+    inst = inst_for(factory(), num_paths=1 << 16, seed=8)
+    out, _, rc = oracle_mod.price(inst)
+    assert rc == 0 and out[2] == 1 << 16
+    se = math.sqrt(out[4] / out[2])
+    r = ref_stats[name]
+    assert abs(out[3] - r["mean"]) < 3 * math.hypot(se, r["se"]), (out[3], r["mean"], se, r["se"])
 
 
 def test_chunk_reduce_matches_fp64_sum(oracle_mod):
