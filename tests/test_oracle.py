@@ -293,6 +293,25 @@ def test_native_price_vs_reference_estimates(oracle_mod, ref_stats, name, factor
     assert abs(out[3] - r["mean"]) < 3 * math.hypot(se, r["se"]), (out[3], r["mean"], se, r["se"])
 
 
+def test_mlmc_level_statistics_vs_reference(oracle_mod, ref_stats):
+    """The oracle's coupled levels of the 2D rainbow (its own Philox draws)
+    against the reference's multilevel_solve statistics at the same levels:
+    the mean of P_f - P_c within 3.5 combined SE, its variance within 30%."""
+    for ref in ref_stats["c2_mlmc_level_stats"]:
+        fine, coarse = ref["levels"]
+        inst = inst_for(indep2d(coarse), num_paths=1 << 14, seed=12, steps=coarse)
+        hf = float(np.float32(1.0) / np.float32(fine))
+        hc = float(np.float32(fine // coarse) * np.float32(hf))
+        out, rc = oracle_mod.mlmc_level(inst, fine // coarse, hf, hc)
+        assert rc == 0 and out[2] == 1 << 14
+        n = out[2]
+        mean = out[0] / n
+        var = (out[1] - out[0] ** 2 / n) / (n - 1)
+        se = math.sqrt(var / n + ref["var"] / ref["n"])
+        assert abs(mean - ref["mean"]) < 3.5 * se, (fine, coarse, mean, ref["mean"], se)
+        assert var == pytest.approx(ref["var"], rel=0.3)
+
+
 def test_chunk_reduce_matches_fp64_sum(oracle_mod):
     rng = np.random.default_rng(0)
     v = rng.random(1000).astype(np.float32)
