@@ -48,3 +48,17 @@ def test_clock_record_parser():
 def test_peak_fallbacks_are_the_stated_measurements():
     assert bench.HBM_FALLBACK_GBS == 6800.0 and bench.BF16_FALLBACK_TFLOPS == 1900.0
     assert bench.load_json_file("no_such_file.json") is None
+
+
+def test_reference_arm_runs_on_rank_zero_only():
+    """Under torchrun the reference arm is rank 0's: another rank exits 0
+    at once, with no output and no process group."""
+    import os
+    import subprocess
+    import sys
+    env = dict(os.environ, RANK="1", WORLD_SIZE="2", LOCAL_RANK="1")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference", "--steps", "1",
+                          "--warmup", "0"], env=env, cwd=root, capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.strip() == ""
