@@ -240,7 +240,10 @@ int sdemc_price_f64(const sdemc_inst* h_inst, void* d_scratch, size_t scratch_by
  * than SDEMC_NOALLOC_MAX_PATHS paths fail with SDEMC_ENOMEM.  The first call
  * on each device looks up the array's device address (cudaGetSymbolAddress)
  * with that device current, so make that first call before any stream
- * capture.  All calls share the one array: calls that overlap on the GPU
+ * capture; the address is kept per CUDA context, and the first call after the
+ * context changes (cudaDeviceReset, or another context made current on that
+ * device) looks it up again, so it too belongs outside a capture.  All calls
+ * share the one array: calls that overlap on the GPU
  * (different streams, or different host threads, on one device) race and
  * must be serialised by the caller.  Nothing here calls cudaMalloc/cudaFree. */
 #define SDEMC_NOALLOC_MAX_PATHS (1 << 23)

@@ -32,12 +32,28 @@ def sources():
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
 
 
-def _compile(nvcc, src, extra):
+def _deps_mtime():
+    """Newest modification time of the headers every translation unit may include."""
+    hdrs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    hdrs.append(os.path.join(HERE, "..", "include", "sdemc.h"))
+    return max(os.path.getmtime(h) for h in hdrs if os.path.exists(h))
+
+
+def _compile(nvcc, src, extra, deps_mtime):
     obj = os.path.join(OBJDIR, os.path.basename(src)[:-3] + ".o")
     cmd = [nvcc, *ARCH, *NVCC_FLAGS, *extra, "-c", src, "-o", obj]
+    stamp = obj + ".cmd"
+    # an object is reused when it is newer than its source and every header and
+    # was built by the same command line
+    if (os.path.exists(obj) and os.path.exists(stamp)
+            and os.path.getmtime(obj) > max(os.path.getmtime(src), deps_mtime)
+            and open(stamp).read() == " ".join(cmd)):
+        return obj, ""
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError("nvcc failed on %s:\n%s\n%s" % (src, " ".join(cmd), res.stderr))
+    with open(stamp, "w") as f:
+        f.write(" ".join(cmd))
     return obj, res.stderr
 
 
@@ -47,8 +63,9 @@ def build(verbose=False, extra=()):
     os.makedirs(OBJDIR, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     srcs = sources()
+    deps = _deps_mtime()
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 4))) as ex:
-        results = list(ex.map(lambda s: _compile(nvcc, s, list(extra)), srcs))
+        results = list(ex.map(lambda s: _compile(nvcc, s, list(extra), deps), srcs))
     if verbose:
         for obj, err in results:
             if err.strip():

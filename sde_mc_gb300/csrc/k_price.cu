@@ -8,100 +8,10 @@
 // warp round) is reduced by a fixed xor butterfly in FP32 and stored as
 // (sum, sum_sq, n) in FP64 at its own slot, so the bits never depend on the
 // grid shape; K10 then sums the slots in a fixed order.
+#include <cuda.h>  // CUcontext / CUresult types only: the library does not link libcuda
 #include <mutex>
 
-#include "sdemc_device.cuh"
-#include "sdemc_host.cuh"
-
-namespace sdemc {
-
-struct PriceParams {
-  sdemc_inst I;
-  RoundKeys rk;
-};
-
-// Payoff of lane path p (terminal state x) and the chunk's FP32 butterfly
-// sums, stored as chunk c's FP64 partial.
-template <int D>
-SDEMC_DI void emit_chunk(const sdemc_inst& I, const float* x, int64_t p, int64_t c, double* part,
-                         float* payoffs) {
-  const int lane = threadIdx.x & 31;
-  const bool valid = p < I.num_paths;
-  const float pay = __fmul_rn(payoff<D>(I, x), I.discount);
-  const float v = valid ? pay : 0.f;
-  if (valid && payoffs) payoffs[p] = pay;
-  const float s = warp_sum(v);
-  const float s2 = warp_sum(__fmul_rn(v, v));
-  const int n = __popc(__ballot_sync(kFull, valid));
-  if (lane == 0) {
-    part[c * 3 + 0] = (double)s;
-    part[c * 3 + 1] = (double)s2;
-    part[c * 3 + 2] = (double)n;
-  }
-}
-
-// PATHS = paths per lane: 1, or 2 (chunks c and c + 1 stepped together by
-// simulate2; the same bits per chunk).
-template <int D, int NOISE, int MODE, int PATHS>
-__global__ void __launch_bounds__(256)
-price_kernel(const __grid_constant__ PriceParams P, double* __restrict__ part,
-             float* __restrict__ payoffs, int32_t* __restrict__ status, int64_t nchunks,
-             int max_iters) {
-  const sdemc_inst& I = P.I;
-  const int lane = threadIdx.x & 31;
-  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  bool ovf = false;
-  for (int64_t c = warp * PATHS; c < nchunks; c += nwarps * PATHS) {
-    const int64_t p = c * kChunk + lane;
-    if (PATHS == 1) {
-      NativeDraws<D, NOISE> dr;
-      dr.init(I, (uint64_t)p, ConstKeys{&P.rk});
-      NullSink sk;
-      float x[D];
-      simulate<D, NOISE, MODE>(I, dr, sk, x, max_iters, ovf);
-      emit_chunk<D>(I, x, p, c, part, payoffs);
-    } else {
-      // the partner chunk c + 1 may lie past the end: its paths run (beyond
-      // num_paths, like the tail lanes of a last chunk) and are not stored
-      const int64_t pb = p + kChunk;
-      NativeDraws<D, NOISE> da, db;
-      da.init(I, (uint64_t)p, ConstKeys{&P.rk});
-      db.init(I, (uint64_t)pb, ConstKeys{&P.rk});
-      float xa[D], xb[D];
-      simulate2<D, NOISE, MODE>(I, da, db, xa, xb, max_iters, ovf);
-      emit_chunk<D>(I, xa, p, c, part, payoffs);
-      if (c + 1 < nchunks) emit_chunk<D>(I, xb, pb, c + 1, part, payoffs);
-    }
-  }
-  if (ovf) atomicOr(status, SDEMC_EOVERFLOW);
-}
-
-template <int D, int NOISE, int MODE>
-static int launch_price_t(const sdemc_inst& I, const sdemc_cfg& cfg, double* part,
-                          float* payoffs, int32_t* status, int64_t nchunks, cudaStream_t s) {
-  const int paths = cfg.interleave == 2 ? 2 : 1;
-  auto kern = paths == 2 ? price_kernel<D, NOISE, MODE, 2> : price_kernel<D, NOISE, MODE, 1>;
-  const int threads = cfg.block_threads > 0 ? cfg.block_threads : 128;
-  int per_sm = 0;
-  int rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0),
-                      "occupancy query");
-  if (rc) return rc;
-  if (cfg.ctas_per_sm > 0 && cfg.ctas_per_sm < per_sm) per_sm = cfg.ctas_per_sm;
-  if (per_sm < 1) per_sm = 1;
-  const int64_t resident = (int64_t)num_sms() * per_sm;
-  const int64_t chunks_per_cta = threads / 32 * paths;
-  int64_t ctas = (nchunks + chunks_per_cta - 1) / chunks_per_cta;
-  if (ctas > resident) ctas = resident;
-  if (ctas < 1) ctas = 1;
-  PriceParams P;
-  P.I = I;
-  P.rk = make_round_keys(I.seed);
-  kern<<<(unsigned)ctas, threads, 0, s>>>(P, part, payoffs, status, nchunks, max_iterations(&I));
-  return check_cuda(cudaGetLastError(), "price_kernel launch");
-}
-
-}  // namespace sdemc
+#include "k_price_kern.cuh"
 
 using namespace sdemc;
 
@@ -132,15 +42,18 @@ extern "C" int sdemc_price_chunks(const sdemc_inst* h_inst, const sdemc_cfg* h_c
   if (nch == 0) return SDEMC_OK;
   const bool exact = (cfg.flags & SDEMC_CFG_EXACT_EULER) != 0;
   const bool nominal = (I.flags & SDEMC_INST_PAYOFF_AT_NOMINAL_STEP) != 0;
-#define SDEMC_PRICE_CASE(D_, N_)                                                                   \
-  rc = nominal ? (exact ? launch_price_t<D_, N_, kModeExact | kModeNominal>(I, cfg, part, d_payoffs, \
-                                                                          status, nch, s)          \
-                        : launch_price_t<D_, N_, kModeNominal>(I, cfg, part, d_payoffs, status,   \
-                                                               nch, s))                           \
-               : (exact ? launch_price_t<D_, N_, kModeExact>(I, cfg, part, d_payoffs, status, nch, s) \
-                        : launch_price_t<D_, N_, 0>(I, cfg, part, d_payoffs, status, nch, s));
-  SDEMC_DISPATCH(I.dim, I.noise, SDEMC_PRICE_CASE)
-#undef SDEMC_PRICE_CASE
+  switch (I.noise) {
+    case SDEMC_NOISE_DIAG:
+      rc = launch_price_noise<SDEMC_NOISE_DIAG>(I, cfg, exact, nominal, part, d_payoffs, status, nch, s);
+      break;
+    case SDEMC_NOISE_INDEP_SHARED:
+      rc = launch_price_noise<SDEMC_NOISE_INDEP_SHARED>(I, cfg, exact, nominal, part, d_payoffs, status, nch, s);
+      break;
+    case SDEMC_NOISE_INDEP_PAIR:
+      rc = launch_price_noise<SDEMC_NOISE_INDEP_PAIR>(I, cfg, exact, nominal, part, d_payoffs, status, nch, s);
+      break;
+    default: return fail(SDEMC_EINVAL, "noise layout %d unknown", I.noise);
+  }
   return rc;
 }
 
@@ -178,12 +91,51 @@ static constexpr size_t kNoallocScratchBytes = scratch_bytes_for(kNoallocMaxChun
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
 
-// Device address of g_noalloc_scratch, looked up once per device.  In host code
-// the symbol is only a host-side stand-in, so the address must come from
-// cudaGetSymbolAddress with that device current.
+// Device address of g_noalloc_scratch, looked up once per CUDA context.  In
+// host code the symbol is only a host-side stand-in, so the address must come
+// from cudaGetSymbolAddress with the device current.  The module (and so the
+// array) is loaded per context: after cudaDeviceReset, or under another
+// context made current on the same device, it lives at a new address.  The
+// cache therefore keeps, per device, the unique id of the context the address
+// belongs to (cuCtxGetId, reached through cudaGetDriverEntryPointByVersion so
+// that the library needs no link to libcuda) and looks the address up again
+// when the current context differs.
 static constexpr int kNoallocMaxDevices = 64;
-static void* g_noalloc_addr[kNoallocMaxDevices] = {};
+struct NoallocAddr {
+  unsigned long long ctx_id;  // 0: nothing cached
+  void* addr;
+};
+static NoallocAddr g_noalloc_addr[kNoallocMaxDevices] = {};
 static std::mutex g_noalloc_mutex;
+
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+
+// Unique id of the calling thread's current context, 0 when none is current
+// (the runtime has not set one up yet) or the driver cannot tell.
+static unsigned long long current_context_id() {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static bool resolved = false;
+  if (!resolved) {  // called with g_noalloc_mutex held
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = (CtxGetCurrentFn)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (CtxGetIdFn)f;
+    resolved = true;
+  }
+  if (!get_current || !get_id) return 0;
+  CUcontext ctx = nullptr;
+  if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+  unsigned long long id = 0;
+  if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 static int noalloc_scratch_address(void** out) {
   int dev = 0;
@@ -191,13 +143,19 @@ static int noalloc_scratch_address(void** out) {
   if (rc) return rc;
   if (dev < 0 || dev >= kNoallocMaxDevices) return fail(SDEMC_EINVAL, "device %d out of range", dev);
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_addr[dev]) {
-    void* p = nullptr;
-    rc = check_cuda(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(no-alloc scratch)");
-    if (rc) return rc;
-    g_noalloc_addr[dev] = p;
+  const unsigned long long ctx = current_context_id();
+  NoallocAddr& c = g_noalloc_addr[dev];
+  if (ctx != 0 && c.ctx_id == ctx && c.addr) {
+    *out = c.addr;
+    return SDEMC_OK;
   }
-  *out = g_noalloc_addr[dev];
+  void* p = nullptr;
+  rc = check_cuda(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress(no-alloc scratch)");
+  if (rc) return rc;
+  // the lookup makes the runtime's context current if none was: key by it
+  c.ctx_id = ctx != 0 ? ctx : current_context_id();
+  c.addr = p;
+  *out = p;
   return SDEMC_OK;
 }
 

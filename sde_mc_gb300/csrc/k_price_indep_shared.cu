@@ -1,0 +1,7 @@
+// k_price_indep_shared.cu — K1 kernels of the indep shared noise layout (every dimension and
+// loop variant), compiled apart from the other layouts so they build in parallel.
+#include "k_price_kern.cuh"
+
+namespace sdemc {
+template SDEMC_PRICE_NOISE_SIG(SDEMC_NOISE_INDEP_SHARED);
+}  // namespace sdemc

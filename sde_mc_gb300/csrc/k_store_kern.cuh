@@ -1,0 +1,306 @@
+// k_store_kern.cuh — the kernels of K4 (materialised paths) and K3 (replay
+// of recorded draws), shared by the translation units that instantiate them:
+// k_store_diag.cu, k_store_indep_shared.cu and k_store_indep_pair.cu each
+// compile the kernels of one noise layout (so the three compile in
+// parallel), and k_store.cu holds the entry points.
+#pragma once
+#include "sdemc_device.cuh"
+#include "sdemc_host.cuh"
+
+namespace sdemc {
+
+struct StoreParams {
+  sdemc_inst I;
+  RoundKeys rk;
+};
+
+// AdaptedPathData stores through shared memory.  A path's rows are contiguous
+// in every array, so a lane writing its own row at each step touches one
+// 32-byte sector per lane and array for a few bytes; instead each lane
+// parks kT steps of (paths, left, jumps, time, normals) in its warp's tile and
+// the warp then writes lane after lane's kT-row segments with consecutive
+// lanes on consecutive addresses (full sectors, a few lines per store
+// instruction).  The padding rows after the loop (the terminal state repeated
+// to S, zero normals) go the same way.  Called in lock-step: k is the same in
+// every lane of the warp.
+template <int D, int NW>
+struct TiledStoreSink {
+  static constexpr bool kWantsLeft = true;
+  static constexpr int kT = (16 / D) > 2 ? 16 / D : 2;  // rows per tile: >= 64 B of a path's state
+  static constexpr int kRowW = 3 * D + 1;             // paths, left, jumps (D each), time
+  static constexpr int kNw = D * NW;                  // normals per step
+  static constexpr int kW = kRowW + kNw;
+  static constexpr int kLaneStride = kT * kW + 1;  // odd: a lane's writes and the flush reads spread over banks
+  static constexpr int kTileFloats = 32 * kLaneStride;
+  float *paths, *left, *time, *jumps, *normals;
+  float* tile;       // this warp's 32 lanes x (kT x kW + 1) floats
+  int64_t p0;        // path of lane 0
+  int64_t n;         // num_paths
+  int S;
+
+  SDEMC_DI float& at(int kk, int lane, int f) const { return tile[lane * kLaneStride + kk * kW + f]; }
+
+  template <int Dd> SDEMC_DI void init(const float* x) {
+    const int64_t p = p0 + (threadIdx.x & 31);
+    if (p >= n) return;
+    const size_t row = (size_t)p * (S + 1);
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      if (paths) paths[row * D + i] = x[i];
+      if (left) left[row * D + i] = x[i];
+      if (jumps) jumps[row * D + i] = 0.f;
+    }
+    if (time) time[row] = 0.f;
+  }
+
+  // One array's segments: every lane's rows [r0, r0 + cnt) of width W, from
+  // tile column f0 on.  CNT > 0: a full tile (cnt = CNT, so the index
+  // arithmetic divides by constants); CNT = 0: a partial tile of cnt rows.
+  template <int W, int CNT>
+  SDEMC_DI void put(float* base, int rows, int f0, int r0, int cnt) const {
+    if (!base) return;
+    const int lane = threadIdx.x & 31;
+    constexpr int SEG = CNT * W;
+    if (CNT > 0 && SEG <= 32 && (32 % (SEG > 0 ? SEG : 1)) == 0) {
+      // a full tile whose segments tile the warp: every lane keeps one
+      // (row, column) of the segment and walks the paths
+      constexpr int PPI = 32 / (SEG > 0 ? SEG : 1);  // paths per store instruction
+      const int q = lane % SEG, kk = q / W, f = q - kk * W;
+      const int jl = lane / SEG;
+      const int soff = kk * kW + f0 + f;
+      float* dst = base + ((size_t)(p0 + jl) * rows + r0 + kk) * W + f;
+      const size_t step = (size_t)PPI * rows * W;
+#pragma unroll
+      for (int it = 0; it < SEG; ++it) {
+        const int j = it * PPI + jl;
+        if (p0 + j < n) *dst = tile[j * kLaneStride + soff];
+        dst += step;
+      }
+      return;
+    }
+    const int seg = (CNT > 0 ? CNT : cnt) * W;
+#pragma unroll 4
+    for (int e = lane; e < 32 * seg; e += 32) {
+      const int j = e / seg, r = e - j * seg, kk = r / W, f = r - kk * W;
+      const int64_t p = p0 + j;
+      if (p < n) base[((size_t)p * rows + r0 + kk) * W + f] = at(kk, j, f0 + f);
+    }
+  }
+
+  template <int CNT>
+  SDEMC_DI void flush(int k0, int cnt) const {
+    __syncwarp();
+    put<D, CNT>(paths, S + 1, 0, k0 + 1, cnt);
+    put<D, CNT>(left, S + 1, D, k0 + 1, cnt);
+    put<D, CNT>(jumps, S + 1, 2 * D, k0 + 1, cnt);
+    put<1, CNT>(time, S + 1, 3 * D, k0 + 1, cnt);
+    put<kNw, CNT>(normals, S, kRowW, k0, cnt);
+    __syncwarp();
+  }
+
+  template <int Dd, int NWd>
+  SDEMC_DI void step(int k, const float* xl, const float* x, float t, float J, int sel,
+                     const float* dW, const float* dW2, const float*, int jump_one) {
+    if (k >= S) return;
+    const int lane = threadIdx.x & 31, kk = k % kT;
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      at(kk, lane, i) = x[i];
+      at(kk, lane, D + i) = xl[i];
+      at(kk, lane, 2 * D + i) = (jump_one && i != sel) ? 0.f : J;
+      if (NW == 1) {
+        at(kk, lane, kRowW + i) = dW[i];
+      } else {
+        at(kk, lane, kRowW + 2 * i) = dW[i];
+        at(kk, lane, kRowW + 2 * i + 1) = dW2[i];
+      }
+    }
+    at(kk, lane, 3 * D) = t;
+    if (kk == kT - 1) flush<kT>(k - kk, kT);
+  }
+
+  // Rows kend .. S-1: the rest of the last tile, then the terminal state (x,
+  // x, 0, t) repeated with zero normals, tile by tile.
+  template <int Dd, int NWd>
+  SDEMC_DI void finish(int kend, const float* x, float t) {
+    const int lane = threadIdx.x & 31;
+    if (kend > S) kend = S;
+    int k = kend;
+    if (k % kT != 0) {
+      // complete the open tile with padding rows, then write it
+      const int k0 = k - k % kT;
+      const int stop = min(S, k0 + kT);
+      for (; k < stop; ++k) fill_row(k % kT, lane, x, t);
+      flush<0>(k0, stop - k0);
+    }
+    if (k < S) {
+      for (int kk = 0; kk < kT; ++kk) fill_row(kk, lane, x, t);
+      for (; k + kT <= S; k += kT) flush<kT>(k, kT);
+      if (k < S) flush<0>(k, S - k);
+    }
+  }
+
+  SDEMC_DI void fill_row(int kk, int lane, const float* x, float t) const {
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      at(kk, lane, i) = x[i];
+      at(kk, lane, D + i) = x[i];
+      at(kk, lane, 2 * D + i) = 0.f;
+    }
+    at(kk, lane, 3 * D) = t;
+#pragma unroll
+    for (int i = 0; i < kNw; ++i) at(kk, lane, kRowW + i) = 0.f;
+  }
+};
+
+template <int D, int NOISE, int MODE>
+__global__ void __launch_bounds__(128)
+materialise_kernel(const __grid_constant__ StoreParams P, int S, float* paths, float* left,
+                   float* time, float* jumps, float* normals, float* payoffs, int32_t* steps,
+                   float* zout, int zdim, float* jt, float* jm, int32_t* jsel, int jcap,
+                   int32_t* status, int max_iters) {
+  using L = Layout<D, NOISE>;
+  using Tiled = TiledStoreSink<D, L::NW>;
+  __shared__ float tiles[4][Tiled::kTileFloats];
+  const sdemc_inst& I = P.I;
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = p < I.num_paths;
+  NativeDraws<D, NOISE> dr;
+  dr.init(I, (uint64_t)p, ConstKeys{&P.rk});
+  bool ovf = false;
+  float x[D];
+  const int it = max_iters < S ? max_iters : S;
+  int own;
+  if (!zout) {
+    Tiled sk;
+    sk.paths = paths; sk.left = left; sk.time = time; sk.jumps = jumps; sk.normals = normals;
+    sk.tile = tiles[threadIdx.x >> 5];
+    sk.p0 = p - (threadIdx.x & 31);
+    sk.n = I.num_paths;
+    sk.S = S;
+    own = simulate<D, NOISE, MODE>(I, dr, sk, x, it, ovf);
+  } else {
+    // with the raw draws exported (the oracle's step-by-step check): per-lane rows
+    StoreSink sk{};
+    sk.S = S;
+    sk.zdim = zdim;
+    if (valid) {
+      const size_t row = (size_t)p * (S + 1);
+      sk.paths = paths ? paths + row * D : nullptr;
+      sk.left = left ? left + row * D : nullptr;
+      sk.time = time ? time + row : nullptr;
+      sk.jumps = jumps ? jumps + row * D : nullptr;
+      sk.normals = normals ? normals + (size_t)p * S * D * L::NW : nullptr;
+      sk.z = zout + (size_t)p * S * zdim;
+    }
+    own = simulate<D, NOISE, MODE>(I, dr, sk, x, it, ovf);
+  }
+  if (!valid) return;
+  if (payoffs) payoffs[p] = __fmul_rn(payoff<D>(I, x), I.discount);
+  if (steps) steps[p] = own;
+  if (ovf) atomicOr(status, SDEMC_EOVERFLOW);
+  // Export the jump stream (times, marks, picks) for the oracle: blocks 0, 1,
+  // 2, ... of the path's jump stream, times accumulated as the loop does.
+  if (jcap > 0 && (jt || jm || jsel)) {
+    float nj = inf_f();
+    for (int j = 0; j < jcap; ++j) {
+      JumpDraw d{0.f, 0.f, 0};
+      if (I.rate > 0.f) {
+        d = jump_from_block<D>(I, dr.ps.block(kTagJumps, (uint32_t)j));
+        nj = j == 0 ? d.gap : __fadd_rn(nj, d.gap);
+      }
+      if (jt) jt[(size_t)p * jcap + j] = nj;
+      if (jm) jm[(size_t)p * jcap + j] = d.mark;
+      if (jsel) jsel[(size_t)p * jcap + j] = d.sel;
+    }
+  }
+}
+
+template <int D, int NOISE>
+__global__ void __launch_bounds__(128)
+replay_kernel(const __grid_constant__ sdemc_inst I, int bs, int S, int MJ, const float* jt,
+              const float* dw, const float* marks, const int32_t* asset, float* paths,
+              float* left, float* time, float* jumps, float* payoffs, int32_t* steps,
+              int32_t* status) {
+  using L = Layout<D, NOISE>;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = p < bs;
+  StoreSink sk{};
+  sk.S = S;
+  sk.zdim = 0;
+  ReplayDraws<D, NOISE> dr{};
+  dr.S = 0;
+  dr.MJ = 0;
+  if (valid) {
+    const size_t row = (size_t)p * (S + 1);
+    sk.paths = paths + row * D;
+    sk.left = left ? left + row * D : nullptr;
+    sk.time = time ? time + row : nullptr;
+    sk.jumps = jumps ? jumps + row * D : nullptr;
+    dr.dw = dw + (size_t)p * S * D * L::NW;
+    dr.marks = marks ? marks + (size_t)p * S : nullptr;
+    dr.asset = asset ? asset + (size_t)p * S : nullptr;
+    dr.jt = jt ? jt + (size_t)p * MJ : nullptr;
+    dr.S = S;
+    dr.MJ = jt ? MJ : 0;
+  }
+  dr.overflow = false;
+  bool ovf = false;
+  float x[D];
+  const int own = simulate<D, NOISE, kModeExact>(I, dr, sk, x, S, ovf);
+  if (!valid) return;
+  if (payoffs) payoffs[p] = __fmul_rn(payoff<D>(I, x), I.discount);
+  if (steps) steps[p] = own;
+  if (ovf || dr.overflow) atomicOr(status, SDEMC_EOVERFLOW);
+}
+
+// K4 launch of every dimension and loop variant of one noise layout (zdim is
+// checked by the caller); instantiated once per layout.
+template <int NOISE>
+int launch_materialise_noise(const StoreParams& P, bool nominal, unsigned blocks, int steps_cap, float* d_paths,
+                             float* d_left, float* d_time, float* d_jumps, float* d_normals, float* d_payoffs,
+                             int32_t* d_steps, float* d_z, float* d_jt, float* d_jm, int32_t* d_jsel, int jcap,
+                             int32_t* d_status, int mi, cudaStream_t s) {
+#define SDEMC_MAT_CASE(D_, N_)                                                                      \
+  {                                                                                                 \
+    constexpr int ZD = Layout<D_, N_>::ZD;                                                          \
+    auto kern = nominal ? materialise_kernel<D_, N_, kModeNominal> : materialise_kernel<D_, N_, 0>; \
+    kern<<<blocks, 128, 0, s>>>(P, steps_cap, d_paths, d_left, d_time, d_jumps, d_normals, d_payoffs, \
+                                d_steps, d_z, ZD, d_jt, d_jm, d_jsel, jcap, d_status, mi);           \
+  }
+  SDEMC_DISPATCH_DIM(NOISE, P.I.dim, SDEMC_MAT_CASE)
+#undef SDEMC_MAT_CASE
+  return check_cuda(cudaGetLastError(), "materialise_kernel launch");
+}
+
+// K3 launch of every dimension of one noise layout.
+template <int NOISE>
+int launch_replay_noise(const sdemc_inst& I, unsigned blocks, int bs, int steps_cap, int max_jumps,
+                        const float* d_jump_times, const float* d_dw, const float* d_marks, const int32_t* d_asset,
+                        float* d_paths, float* d_left, float* d_time, float* d_jumps, float* d_payoffs,
+                        int32_t* d_steps, int32_t* d_status, cudaStream_t s) {
+#define SDEMC_REPLAY_CASE(D_, N_)                                                                          \
+  replay_kernel<D_, N_><<<blocks, 128, 0, s>>>(I, bs, steps_cap, max_jumps, d_jump_times, d_dw, d_marks, \
+                                               d_asset, d_paths, d_left, d_time, d_jumps, d_payoffs,     \
+                                               d_steps, d_status);
+  SDEMC_DISPATCH_DIM(NOISE, I.dim, SDEMC_REPLAY_CASE)
+#undef SDEMC_REPLAY_CASE
+  return check_cuda(cudaGetLastError(), "replay_kernel launch");
+}
+
+#define SDEMC_MATERIALISE_NOISE_SIG(N_)                                                                      \
+  int launch_materialise_noise<N_>(const StoreParams&, bool, unsigned, int, float*, float*, float*, float*, \
+                                   float*, float*, int32_t*, float*, float*, float*, int32_t*, int, int32_t*, \
+                                   int, cudaStream_t)
+#define SDEMC_REPLAY_NOISE_SIG(N_)                                                                            \
+  int launch_replay_noise<N_>(const sdemc_inst&, unsigned, int, int, int, const float*, const float*,         \
+                              const float*, const int32_t*, float*, float*, float*, float*, float*, int32_t*, \
+                              int32_t*, cudaStream_t)
+extern template SDEMC_MATERIALISE_NOISE_SIG(SDEMC_NOISE_DIAG);
+extern template SDEMC_MATERIALISE_NOISE_SIG(SDEMC_NOISE_INDEP_SHARED);
+extern template SDEMC_MATERIALISE_NOISE_SIG(SDEMC_NOISE_INDEP_PAIR);
+extern template SDEMC_REPLAY_NOISE_SIG(SDEMC_NOISE_DIAG);
+extern template SDEMC_REPLAY_NOISE_SIG(SDEMC_NOISE_INDEP_SHARED);
+extern template SDEMC_REPLAY_NOISE_SIG(SDEMC_NOISE_INDEP_PAIR);
+
+}  // namespace sdemc

@@ -337,7 +337,7 @@ def heston_asian_fixtures(sm, torch):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('--ref', default='/root/reference')
+    ap.add_argument('--ref', required=True, help='checkout of the sde_mc reference to import')
     ap.add_argument('--skip-stats', action='store_true')
     ap.add_argument('--only', choices=['cv_jumps', 'heston_asian', 'diffusions', 'levy_mlmc', 'model_stats'],
                     default=None,
