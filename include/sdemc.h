@@ -515,6 +515,42 @@ typedef struct {
   double busy_s;            /* sum of tick durations on the device              */
 } sdemc_server_stats;
 
+/* Integrand-weight parameters of SDEMC_EST_LINEAR_CV for one descriptor, as
+ * the server derives them at admission.  w(t, X) = N(d1) (call-like) or
+ * N(d1) - 1 (puts) with d1 = (ln A + drift tau) inv_sig / sqrt(tau), A =
+ * scale_over_k * agg(X) (agg 0: asset 0, 1: mean, 2: max), tau = T - t, and
+ * g(t, X) = A inv_sig phi(d1) / sqrt(tau); wkind 0 means w = g = 1.  comp[i]
+ * is the jump compensator rate lambda_i E[J] of asset i, comp_j2 = lambda
+ * E[J^2]; inv_comp / inv_comp_j2 are their float reciprocals (0 for a zero
+ * rate); jumps = 1 when the jump regressors are on (lognormal marks).     */
+typedef struct sdemc_cv_weights {
+  float comp[SDEMC_MAX_DIM];
+  float inv_comp[SDEMC_MAX_DIM];
+  float scale_over_k, inv_sig, drift, T, comp_j2, inv_comp_j2;
+  int32_t agg, wkind, jumps;
+  int32_t reserved;
+} sdemc_cv_weights;
+
+/* Host only: the weight parameters the server uses for *h_inst.           */
+int sdemc_serve_cv_weights(const sdemc_inst* h_inst, sdemc_cv_weights* h_out);
+
+/* The served control variate path by path, for checking it against an
+ * independent restatement: runs the server kernels' per-path code (the same
+ * loop, draws and regressor accumulation) on paths [0, num_paths) of *h_inst
+ * (diagonal noise, terminal payoff) and writes each path's discounted payoff
+ * d_payoff (n) and its 2d + 1 regressors d_reg (n, 2d + 1).  Optional
+ * exports (nullable): the raw draws as sdemc_materialise exports them (d_z
+ * (n, steps_cap, dim) standard normals, d_jt / d_jm / d_jsel (n, jcap) the
+ * jump stream) and the integrand weights evaluated at the start of every
+ * 4-step block, d_wg (n, wcap, 2) as (w, g).  Steps past steps_cap or blocks
+ * past wcap are not exported and set SDEMC_EOVERFLOW in *d_status.  No
+ * reference function computes these regressors; their estimator stands in
+ * for run_mc's plain estimate (sde_mc/mc.py:418-440), with the pilot's
+ * variance sizing the main run as find_num_trials does (:418-427).        */
+int sdemc_serve_cv_paths(const sdemc_inst* h_inst, int steps_cap, float* d_payoff, float* d_reg,
+                         float* d_z, float* d_jt, float* d_jm, int32_t* d_jsel, int jcap,
+                         float* d_wg, int wcap, int32_t* d_status, void* stream);
+
 int sdemc_server_create(const sdemc_server_cfg* cfg, sdemc_server** out);
 /* Enqueue one request (thread-safe; arrival time = now).  Rejects invalid
  * descriptors and requests that could never fit the budget.               */

@@ -12,6 +12,10 @@ Contents (each restating the reference, piers-hinds/sde_mc):
     geometric Asian and the 40-term Merton series (sde_mc/options.py:8-153);
   * mc_estimates (sde_mc/helpers.py:51-68) and Giles' MLMC allocation
     (sde_mc/mlmc.py:77-97);
+  * the pricing server's request flow (run_mc, sde_mc/mc.py:418-440, with the
+    linear control variate): per-path regressors in C, then the pilot sums,
+    the regression for beta, the main-run size (find_num_trials,
+    sde_mc/mc.py:418-427) and the main run's sums;
   * the control-variate MLP (sde_mc/nets.py:39-93 without batch norm), its
     variance loss (sde_mc/varred.py:160-177, 202-214) with hand-derived
     gradients, and one Adam step, in numpy FP64.
@@ -52,6 +56,10 @@ def load():
             "oracle_mlmc_level": (I, [P, I, F, F, I, P, P]),
             "oracle_chunk_reduce": (None, [P, P, I64, P]),
             "oracle_payoff": (F, [P, P]),
+            "oracle_serve_cv_weights": (I, [P, P]),
+            "oracle_serve_cv_from_export": (I, [P, P, I64, I, P, P, P, P, I, P, I, P, P, P]),
+            "oracle_serve_rows": (None, [I, I64, P, P, P, P]),
+            "oracle_serve_slices": (None, [P, I64, I, I64, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -406,3 +414,169 @@ def cv2_loss_and_grads(pf, pg, time, paths, left, normals, mult_g, payoffs, r):
     loss, gamma, gf = cv_loss_and_grads(pf, fin, np.asarray(normals, np.float64), t, pay + a_g, r)
     _, _, gg = cv_loss_and_grads(pg, gin, mult_g, t, pay + a_f, r)
     return loss, gamma, gf, gg
+
+
+# ------------------------------------------------- served control variate ---
+class CvWeights(ctypes.Structure):
+    """Mirror of ``sdemc_cv_weights`` (include/sdemc.h)."""
+    _fields_ = [("comp", ctypes.c_float * 8), ("inv_comp", ctypes.c_float * 8), ("scale_over_k", ctypes.c_float),
+                ("inv_sig", ctypes.c_float), ("drift", ctypes.c_float), ("T", ctypes.c_float),
+                ("comp_j2", ctypes.c_float), ("inv_comp_j2", ctypes.c_float), ("agg", ctypes.c_int32),
+                ("wkind", ctypes.c_int32), ("jumps", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+def serve_cv_weights(inst):
+    cw = CvWeights()
+    rc = load().oracle_serve_cv_weights(ctypes.byref(inst), ctypes.byref(cw))
+    assert rc == 0
+    return cw
+
+
+def serve_cv_from_export(inst, cw, z, jt=None, jm=None, jsel=None, wg=None):
+    """Per-path payoffs and the 2d + 1 control-variate regressors re-run from a
+    GPU run's exported draws.  With ``wg`` (n, wcap, 2) the GPU's weights are
+    used and checked: returns (payoffs, reg, rc, (worst w ratio, worst g
+    ratio, blocks)); the ratios are error / bound and must stay <= 1."""
+    z = _c(z)
+    n, S = z.shape[0], z.shape[1]
+    R = 2 * inst.dim + 1
+    jt, jm, jsel, wg = _c(jt), _c(jm), _c(jsel, np.int32), _c(wg)
+    jcap = jt.shape[1] if jt is not None else 0
+    wcap = wg.shape[1] if wg is not None else 0
+    pay = np.zeros(n, np.float32)
+    reg = np.zeros((n, R), np.float32)
+    ws = np.zeros(3, np.float64)
+    rc = load().oracle_serve_cv_from_export(ctypes.byref(inst), ctypes.byref(cw), n, S, _p(z), _p(jt), _p(jm),
+                                            _p(jsel), jcap, _p(wg), wcap, _p(pay), _p(reg), _p(ws))
+    return pay, reg, rc, tuple(ws)
+
+
+def serve_rows(pv, y, beta=None):
+    """The server kernels' per-chunk FP64 rows (see oracle_serve_rows)."""
+    pv, y = _c(pv), _c(y)
+    n, R = y.shape
+    W = 3 if beta is not None else 3 + 2 * R + R * (R + 1) // 2
+    nch = (n + 31) // 32
+    rows = np.zeros((max(nch, 1), W), np.float64)
+    b = None if beta is None else _c(np.asarray(beta, np.float32)[:R])
+    load().oracle_serve_rows(R, n, _p(pv), _p(y), _p(b), _p(rows))
+    return rows[:nch]
+
+
+def serve_slices(rows, slice_paths):
+    """A phase's running sums: the rows accumulated slice by slice."""
+    rows = _c(rows, np.float64)
+    nch, W = rows.shape
+    acc = np.zeros(W, np.float64)
+    load().oracle_serve_slices(_p(rows), nch, W, slice_paths // 32, _p(acc))
+    return acc
+
+
+def serve_slice_paths(inst, slice_work=1 << 28):
+    """Paths per slice of a request: the slice work over the expected path
+    cost (nominal steps plus expected jumps, times the dimension), clamped to
+    [2^10, 2^18] and rounded up to whole 32-path chunks."""
+    steps = float(inst.num_steps)
+    if inst.grid == 0:
+        steps += float(np.float32(inst.rate)) * float(np.float32(inst.T))
+    cost = steps * float(inst.dim)
+    sl = math.ceil(float(slice_work) / max(cost, 1.0))
+    sl = min(max(sl, 1 << 10), 1 << 18)
+    return (sl + 31) // 32 * 32
+
+
+def _solve_spd(C, c):
+    """Cholesky solve of C beta = c with a jitter of 1e-12 tr / d on the
+    diagonal, in the server's operation order; None when C is degenerate."""
+    d = len(c)
+    tr = 0.0
+    for i in range(d):
+        tr += C[i][i]
+    if not (tr > 0.0) or not math.isfinite(tr):
+        return None
+    jitter = 1e-12 * tr / d
+    L = [[0.0] * d for _ in range(d)]
+    for i in range(d):
+        for j in range(i + 1):
+            s = C[i][j] + (jitter if i == j else 0.0)
+            for k in range(j):
+                s -= L[i][k] * L[j][k]
+            if i == j:
+                if not (s > 0.0):
+                    return None
+                L[i][i] = math.sqrt(s)
+            else:
+                L[i][j] = s / L[j][j]
+    z = [0.0] * d
+    for i in range(d):
+        s = c[i]
+        for k in range(i):
+            s -= L[i][k] * z[k]
+        z[i] = s / L[i][i]
+    beta = [0.0] * d
+    for i in range(d - 1, -1, -1):
+        s = z[i]
+        for k in range(i + 1, d):
+            s -= L[k][i] * beta[k]
+        beta[i] = s / L[i][i]
+    if not all(math.isfinite(b) for b in beta):
+        return None
+    return beta
+
+
+def serve_fit(acc, R, rel_target, max_paths=0):
+    """A finished pilot: its mean and standard error, the control variate's
+    coefficients fitted by regression on the pilot sums (kept when they cut
+    the variance by 5 % or more), and the main run's size for a 95 %
+    half-width of rel_target x |price| (find_num_trials, sde_mc/mc.py:418-427).
+    acc holds the pilot sums in the pilot-statistics layout (or 3 sums for a
+    plain pilot, R = 0)."""
+    n = acc[2]
+    mean = acc[0] / n if n > 0 else 0.0
+    var = max((acc[1] - acc[0] * acc[0] / n) / (n - 1.0), 0.0) if n > 1 else 0.0
+    out = dict(pilot_mean=mean, pilot_se=math.sqrt(var / max(n, 1.0)), est=0, vrf=1.0,
+               beta=np.zeros(17, np.float32))
+    var_main = var
+    if R > 0 and n > 2:
+        ybar = [acc[3 + a] / n for a in range(R)]
+        C = [[0.0] * R for _ in range(R)]
+        q = 3 + R
+        for a in range(R):
+            for b in range(a, R):
+                v = (acc[q] - n * ybar[a] * ybar[b]) / (n - 1.0)
+                C[a][b] = v
+                C[b][a] = v
+                q += 1
+        c = [(acc[q + a] - n * ybar[a] * mean) / (n - 1.0) for a in range(R)]
+        beta = _solve_spd(C, c)
+        if beta is not None:
+            explained = 0.0
+            for a in range(R):
+                explained += beta[a] * c[a]
+            resid = var - explained
+            if 0.0 < resid < var / 1.05:
+                var_main = resid
+                out["est"] = 1
+                out["vrf"] = var / resid
+                out["beta"][:R] = np.asarray(beta, np.float64).astype(np.float32)
+    out["var_main"] = var_main
+    if var_main <= 0.0:
+        out["main_paths"] = 0
+        return out
+    cap = max_paths if max_paths > 0 else (1 << 36)
+    eps = rel_target * abs(mean)
+    if eps > 0.0 and math.isfinite(eps):
+        want = math.ceil(1.96 * 1.96 * var_main / (eps * eps))
+        nmain = cap if want >= cap else int(want)
+    else:
+        nmain = cap
+    out["main_paths"] = max(nmain, 64)
+    return out
+
+
+def serve_main(acc):
+    """Mean and standard error of a finished main run from its 3 sums."""
+    n = acc[2]
+    mean = acc[0] / n if n > 0 else 0.0
+    var = max((acc[1] - acc[0] * acc[0] / n) / (n - 1.0), 0.0) if n > 1 else 0.0
+    return mean, math.sqrt(var / max(n, 1.0))

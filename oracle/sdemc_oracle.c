@@ -347,13 +347,126 @@ float oracle_payoff(const sdemc_inst* I, const float* xin) {
   }
 }
 
+/* ------------------------------------------- served control variate --- */
+/* The pricing server's linear control variate, restated per path: with X_k
+ * the state at the start of step k, dW_k its correlated increment and J the
+ * mark of a jump at the end of the step,
+ *   r_i     = sum_k w_k X^i_k dW^i_k
+ *   r_{d+i} = -comp_i a_i,  a_i = sum_k w_k X^i_k (dt_k - J^i / comp_i)
+ *   r_{2d}  = -comp_j2 ag,  ag  = sum_k g_k (dt_k - J^2 / comp_j2)
+ * i.e. sum_k w_k X^i_k (J^i - comp_i dt_k) and sum_k g_k (J^2 - comp_j2 dt_k):
+ * stochastic integrals of predictable integrands against the Brownian
+ * increments and the compensated jump measures, each with mean zero.  The
+ * weights (w, g) are evaluated at the start of every 4-step block of the
+ * path's own steps.  Operation order as the kernel's, every multiply-add an
+ * fmaf, the reciprocals of the compensator rates taken from the weights.
+ * No reference function computes these; the estimator P - beta . r they
+ * feed replaces run_mc's plain estimate (sde_mc/mc.py:418-440). */
+typedef struct {
+  const sdemc_cv_weights* cw;
+  const float* wg;   /* recorded (w, g) per block, or NULL: evaluate here */
+  int wcap, D, bad;
+  float xp[MAXD], r[MAXD], a[MAXD], tp, w, g, ag;
+  double wstat[3];   /* worst |dw| / bound, worst |dg| / bound, blocks checked */
+} cvacc_t;
+
+/* Normal cdf and density of the weights, from libm's erfcf and expf. */
+static float cv_ncdf(float d1) { return 0.5f * erfcf(-d1 * 0.70710678f); }
+
+/* Evaluate (w, g) at the accumulator's block-start state (xp, tp); d1_out,
+ * is_out and lm_out receive the intermediates (for the error bound). */
+static void cv_eval(const cvacc_t* c, float* w, float* g, float* d1_out, float* is_out, float* lm_out, float* v_out) {
+  const sdemc_cv_weights* cw = c->cw;
+  *d1_out = 0.f; *is_out = 0.f; *lm_out = 0.f; *v_out = 0.f;
+  if (cw->wkind == 0) { *w = 1.f; *g = 1.f; return; }
+  float m = c->xp[0];
+  if (cw->agg == 1) {
+    for (int i = 1; i < c->D; ++i) m = m + c->xp[i];
+    m = m * (1.f / (float)c->D);
+  } else if (cw->agg == 2) {
+    for (int i = 1; i < c->D; ++i) m = fmaxf(m, c->xp[i]);
+  }
+  m = m * cw->scale_over_k;
+  const float tau = fmaxf(cw->T - c->tp, 1e-6f);
+  const float is = (1.f / sqrtf(tau)) * cw->inv_sig;
+  if (m > 0.f) {
+    const float lm = logf(m);
+    const float d1 = fmaf(cw->drift, tau, lm) * is;
+    const float v = cv_ncdf(d1);
+    *w = cw->wkind == 2 ? v - 1.f : v;
+    *g = (m * is) * (0.39894228f * expf(-0.5f * (d1 * d1)));
+    *d1_out = d1; *is_out = is; *lm_out = lm; *v_out = v;
+  } else {
+    *w = cw->wkind == 2 ? -1.f : 0.f;
+    *g = 0.f;
+  }
+}
+
+/* Weights of block b: the recorded ones (each checked against this file's
+ * own evaluation within an error bound) or this file's own. */
+static void cv_weights_block(cvacc_t* c, int b) {
+  float w, g, d1, is, lm, v;
+  cv_eval(c, &w, &g, &d1, &is, &lm, &v);
+  if (!c->wg) { c->w = w; c->g = g; return; }
+  if (b >= c->wcap) { c->bad = 1; c->w = w; c->g = g; return; }
+  const float rw = c->wg[2 * b], rg = c->wg[2 * b + 1];
+  /* The kernel evaluates ln, 1/sqrt, the normal cdf and exp with CUDA's
+   * intrinsics (absolute error of __logf <= 2^-21.41 near 1, otherwise 3 ulp;
+   * rsqrtf 2 ulp; normcdff 5 ulp; __expf 2 + 1.173|x| ulp); propagate those
+   * through d1 = (ln m + drift tau) is, w = N(d1), g = m is phi(d1), with a
+   * factor 2 to spare. */
+  const double ulp = 1.0 / 8388608.0;
+  const double dd1 = fabs((double)is) * (4.0e-7 + 8.0 * ulp * fabs((double)lm)) + fabs((double)d1) * 8.0 * ulp;
+  const double phi = 0.3989422804014327 * exp(-0.5 * (double)d1 * d1);
+  const double bw = 2.0 * (phi * dd1 + 8.0 * ulp * fabs((double)v)) + 1e-12;
+  const double x = 0.5 * (double)d1 * d1;
+  const double bg = 2.0 * fabs((double)g) * (8.0 * ulp + fabs((double)d1) * dd1 + (8.0 + 1.2 * x) * ulp) + 1e-12;
+  const double ew = fabs((double)rw - (double)w) / bw, eg = fabs((double)rg - (double)g) / bg;
+  if (ew > c->wstat[0]) c->wstat[0] = ew;
+  if (eg > c->wstat[1]) c->wstat[1] = eg;
+  c->wstat[2] += 1.0;
+  c->w = rw; c->g = rg;
+}
+
+static void cv_init(cvacc_t* c, const float* x) {
+  for (int i = 0; i < c->D; ++i) { c->xp[i] = x[i]; c->r[i] = 0.f; c->a[i] = 0.f; }
+  c->tp = 0.f; c->ag = 0.f;
+  cv_weights_block(c, 0);
+}
+
+static void cv_step(cvacc_t* c, int k, const float* x, float t, float J, int sel, const float* dW, int jump_one) {
+  const sdemc_cv_weights* cw = c->cw;
+  if (k > 0 && (k & 3) == 0) cv_weights_block(c, k >> 2);
+  for (int i = 0; i < c->D; ++i) c->r[i] = fmaf(c->xp[i], c->w * dW[i], c->r[i]);
+  if (cw->jumps) {
+    const float dt = t - c->tp;
+    const float wdt = c->w * dt;
+    for (int i = 0; i < c->D; ++i) c->a[i] = fmaf(c->xp[i], wdt, c->a[i]);
+    c->ag = fmaf(c->g, dt, c->ag);
+    if (J != 0.f) {
+      for (int i = 0; i < c->D; ++i)
+        if (!jump_one || i == sel) c->a[i] = fmaf(-(c->w * c->xp[i]), J * cw->inv_comp[i], c->a[i]);
+      c->ag = fmaf(-c->g, (J * J) * cw->inv_comp_j2, c->ag);
+    }
+  }
+  for (int i = 0; i < c->D; ++i) c->xp[i] = x[i];
+  c->tp = t;
+}
+
+static float cv_reg(const cvacc_t* c, int q) {
+  const int D = c->D;
+  if (q < D) return c->r[q];
+  if (q < 2 * D) return -(c->cw->comp[q - D] * c->a[q - D]);
+  return -(c->cw->comp_j2 * c->ag);
+}
+
 /* One path of the reference loop.  Storage pointers may be NULL; when given
  * they follow the AdaptedPathData layout with S = cap columns (+1). Returns
  * the path's active step count (or -1 on overflow). A path runs alone here,
  * so "frozen" steps of the batch-global loop are simply not taken; storage
  * columns after the last step hold the frozen values. */
 static int run_path(const sdemc_inst* I, draws_t* d, int exact, int cap, float* paths, float* left,
-                    float* time, float* jumps, float* normals, float* x) {
+                    float* time, float* jumps, float* normals, float* x, cvacc_t* cv) {
   const int D = I->dim, NW = nw_of(I->noise);
   int jump_one = I->jump_target == SDEMC_JUMP_ONE_ASSET;
   for (int i = 0; i < D; ++i) x[i] = I->x0[i];
@@ -361,6 +474,7 @@ static int run_path(const sdemc_inst* I, draws_t* d, int exact, int cap, float* 
   if (left) for (int i = 0; i < D; ++i) left[i] = x[i];
   if (jumps) for (int i = 0; i < D; ++i) jumps[i] = 0.f;
   if (time) time[0] = 0.f;
+  if (cv) cv_init(cv, x);
   float t = 0.f, dW[MAXD], dW2[MAXD], old[MAXD], xl[MAXD];
   int k = 0;
   if (I->grid == SDEMC_GRID_UNIFORM) {
@@ -368,6 +482,7 @@ static int run_path(const sdemc_inst* I, draws_t* d, int exact, int cap, float* 
       draws_increments(I, D, d, k, I->h, dW, dW2);
       euler(I, D, exact, x, I->h, dW, dW2);
       t = t + I->h;
+      if (cv) cv_step(cv, k, x, t, 0.f, 0, dW, 0);
       if (k < cap) {
         size_t c = (size_t)(k + 1) * D;
         if (paths) for (int i = 0; i < D; ++i) paths[c + i] = x[i];
@@ -401,6 +516,7 @@ static int run_path(const sdemc_inst* I, draws_t* d, int exact, int cap, float* 
         apply_jump(I, D, exact, x, I->exact_jumps ? x : old, J, sel);
         nj = draws_jump_next(I, D, d, nj);
       }
+      if (cv) cv_step(cv, k, x, t, J, sel, dW, jump_one);
       size_t c = (size_t)(k + 1) * D;
       if (paths) for (int i = 0; i < D; ++i) paths[c + i] = x[i];
       if (left) for (int i = 0; i < D; ++i) left[c + i] = xl[i];
@@ -478,7 +594,7 @@ int oracle_replay(const sdemc_inst* I, int bs, int S, int MJ, const float* jt, c
     float x[MAXD];
     size_t row = (size_t)p * (S + 1);
     int k = run_path(I, &d, 1, S, paths ? paths + row * D : NULL, left ? left + row * D : NULL,
-                     time ? time + row : NULL, jumps ? jumps + row * D : NULL, NULL, x);
+                     time ? time + row : NULL, jumps ? jumps + row * D : NULL, NULL, x, NULL);
     if (k < 0) bad = 1;
     if (steps) steps[p] = k;
     if (payoffs) payoffs[p] = oracle_payoff(I, x) * I->discount;
@@ -508,12 +624,206 @@ int oracle_from_export(const sdemc_inst* I, int64_t n, int S, const float* z, in
     size_t row = (size_t)p * (S + 1);
     int k = run_path(I, &d, exact, S, paths ? paths + row * D : NULL, left ? left + row * D : NULL,
                      time ? time + row : NULL, jumps ? jumps + row * D : NULL,
-                     normals ? normals + (size_t)p * S * D * NW : NULL, x);
+                     normals ? normals + (size_t)p * S * D * NW : NULL, x, NULL);
     if (k < 0) bad = 1;
     if (steps) steps[p] = k;
     if (payoffs) payoffs[p] = oracle_payoff(I, x) * I->discount;
   }
   return bad ? SDEMC_EOVERFLOW : SDEMC_OK;
+}
+
+/* ------------------------------------------- served control variate --- */
+/* The weight parameters the server derives for a descriptor: the jump
+ * compensator rates lambda_i E[J] (E[J] = exp(alpha + gamma^2/2) - 1 for
+ * lognormal marks; per asset, lambda times the asset's pick probability) and
+ * lambda E[J^2]; the delta kind and aggregate of the payoff; and a lognormal
+ * proxy volatility of the payoff's underlying (the correlated mean's or the
+ * assets' mean variance, plus the jump variance).  All in double, rounded to
+ * float at the end, in the server's operation order. */
+int oracle_serve_cv_weights(const sdemc_inst* I, sdemc_cv_weights* cw) {
+  memset(cw, 0, sizeof(*cw));
+  const int d = I->dim;
+  double jump_var = 0.0;
+  const double a = I->mark_p[0], g = I->mark_p[1];
+  const double kappa = exp(a + 0.5 * g * g) - 1.0;
+  if (I->rate > 0.f && I->mark == SDEMC_MARK_LOGNORMAL && fabs(kappa) > 1e-9) {
+    for (int i = 0; i < d; ++i) {
+      double p = 1.0;
+      if (I->jump_target == SDEMC_JUMP_ONE_ASSET) {
+        const double lo = i > 0 ? I->jump_cdf[i - 1] : 0.0, hi = i < d - 1 ? I->jump_cdf[i] : 1.0;
+        p = hi - lo;
+      }
+      cw->comp[i] = (float)((double)I->rate * p * kappa);
+    }
+    cw->jumps = 1;
+    cw->comp_j2 = (float)((double)I->rate * (exp(2.0 * a + 2.0 * g * g) - 2.0 * exp(a + 0.5 * g * g) + 1.0));
+    jump_var = (double)I->rate * (a * a + g * g) / (I->jump_target == SDEMC_JUMP_ONE_ASSET ? d : 1);
+  }
+  switch (I->payoff) {
+    case SDEMC_PAYOFF_EUROCALL: cw->wkind = 1; cw->agg = 0; break;
+    case SDEMC_PAYOFF_EUROPUT: cw->wkind = 2; cw->agg = 0; break;
+    case SDEMC_PAYOFF_BASKET_ARITH:
+    case SDEMC_PAYOFF_BASKET_GEO: cw->wkind = 1; cw->agg = 1; break;
+    case SDEMC_PAYOFF_RAINBOW:
+    case SDEMC_PAYOFF_BESTOF: cw->wkind = 1; cw->agg = 2; break;
+    default: cw->wkind = 0; break;
+  }
+  if (I->payoff_log || !(I->strike > 0.f)) cw->wkind = 0;
+  double L[MAXD][MAXD];
+  memset(L, 0, sizeof(L));
+  for (int i = 0, q = 0; i < d; ++i)
+    for (int j = 0; j <= i; ++j) L[i][j] = I->chol[q++];
+  double sig[MAXD];
+  for (int i = 0; i < d; ++i) sig[i] = fabs((double)I->diff_q[i]);
+  if (I->model == SDEMC_MODEL_HESTON) sig[0] = sqrt((double)I->x0[1] > 0.0 ? (double)I->x0[1] : 0.0);
+  double var = 0.0;
+  if (cw->agg == 0) {
+    var = sig[0] * sig[0];
+  } else if (cw->agg == 1) {
+    for (int i = 0; i < d; ++i)
+      for (int j = 0; j < d; ++j) {
+        double c = 0.0;
+        for (int k = 0; k < d; ++k) c += L[i][k] * L[j][k];
+        var += sig[i] * sig[j] * c;
+      }
+    var /= (double)d * d;
+  } else {
+    for (int i = 0; i < d; ++i) var += sig[i] * sig[i];
+    var /= d;
+  }
+  var = var + jump_var > 1e-8 ? var + jump_var : 1e-8;
+  cw->inv_sig = (float)(1.0 / sqrt(var));
+  cw->drift = (float)((double)I->disc_rate + 0.5 * var);
+  cw->T = I->T;
+  cw->scale_over_k = cw->wkind ? (float)((double)I->payoff_scale / (double)I->strike) : 1.f;
+  for (int i = 0; i < MAXD; ++i) cw->inv_comp[i] = cw->comp[i] != 0.f ? (float)(1.0 / (double)cw->comp[i]) : 0.f;
+  cw->inv_comp_j2 = cw->comp_j2 != 0.f ? (float)(1.0 / (double)cw->comp_j2) : 0.f;
+  return SDEMC_OK;
+}
+
+/* Re-run paths [0, n) from the raw draws a GPU run exported (z (n, S, dim),
+ * jump stream (n, jcap)) with the control variate accumulated: payoffs (n)
+ * and regressors reg (n, 2 dim + 1).  wg (n, wcap, 2), when given, holds the
+ * weights the GPU evaluated per block: they are used for the accumulation
+ * (so the accumulation is compared bit for bit) and each is checked against
+ * this file's own evaluation; wstat = (worst |dw| / bound, worst |dg| /
+ * bound, blocks checked).  Without wg the weights are this file's own. */
+int oracle_serve_cv_from_export(const sdemc_inst* I, const sdemc_cv_weights* cw, int64_t n, int S, const float* z,
+                                const float* jt, const float* jm, const int32_t* js, int jcap, const float* wg,
+                                int wcap, float* payoffs, float* reg, double* wstat) {
+  const int D = I->dim, R = 2 * D + 1;
+  int bad = 0;
+  if (wstat) { wstat[0] = 0.0; wstat[1] = 0.0; wstat[2] = 0.0; }
+  for (int64_t p = 0; p < n; ++p) {
+    draws_t d;
+    memset(&d, 0, sizeof(d));
+    d.mode = DRAW_EXPORT;
+    d.z = z + (size_t)p * S * D; d.zdim = D; d.S = S;
+    d.xjt = jt ? jt + (size_t)p * jcap : NULL;
+    d.xjm = jm ? jm + (size_t)p * jcap : NULL;
+    d.xjsel = js ? js + (size_t)p * jcap : NULL;
+    d.jcap = jt ? jcap : 0;
+    d.h_nom = I->h; d.sq_h = sqrtf(I->h);
+    cvacc_t c;
+    memset(&c, 0, sizeof(c));
+    c.cw = cw; c.D = D; c.wcap = wcap;
+    c.wg = wg ? wg + (size_t)p * wcap * 2 : NULL;
+    float x[MAXD];
+    int k = run_path(I, &d, 0, S, NULL, NULL, NULL, NULL, NULL, x, &c);
+    if (k < 0 || c.bad) bad = 1;
+    payoffs[p] = oracle_payoff(I, x) * I->discount;
+    for (int q = 0; q < R; ++q) reg[(size_t)p * R + q] = cv_reg(&c, q);
+    if (wstat) {
+      if (c.wstat[0] > wstat[0]) wstat[0] = c.wstat[0];
+      if (c.wstat[1] > wstat[1]) wstat[1] = c.wstat[1];
+      wstat[2] += c.wstat[2];
+    }
+  }
+  return bad ? SDEMC_EOVERFLOW : SDEMC_OK;
+}
+
+/* FP32 xor butterfly over one chunk's 32 lane values (as the kernel's warp sum). */
+static float butterfly(float* v) {
+  float t[32];
+  for (int o = 16; o > 0; o >>= 1) {
+    for (int l = 0; l < 32; ++l) t[l] = v[l] + v[l ^ o];
+    memcpy(v, t, sizeof(t));
+  }
+  return v[0];
+}
+
+/* The server kernels' per-chunk rows over per-path payoffs pv (n) and
+ * regressors y (n, R).  beta == NULL: the pilot-statistics kind, W = 3 + 2R
+ * + R(R+1)/2 columns (sum P, sum P^2, n, sum r_a, sum r_a r_b for a <= b,
+ * sum P r_a); otherwise the control-variate kind, W = 3 over v = P - beta . r
+ * (one fmaf per regressor).  Lanes past n contribute 0. */
+void oracle_serve_rows(int R, int64_t n, const float* pv, const float* y, const float* beta, double* rows) {
+  const int64_t nch = (n + 31) / 32;
+  const int W = beta ? 3 : 3 + 2 * R + R * (R + 1) / 2;
+  float lp[32], ly[32][2 * MAXD + 1], v[32];
+  for (int64_t c = 0; c < nch; ++c) {
+    double* out = rows + (size_t)c * W;
+    int cnt = 0;
+    for (int l = 0; l < 32; ++l) {
+      const int64_t p = c * 32 + l;
+      const int ok = p < n;
+      cnt += ok;
+      lp[l] = ok ? pv[p] : 0.f;
+      for (int i = 0; i < R; ++i) ly[l][i] = ok ? y[(size_t)p * R + i] : 0.f;
+    }
+    if (beta) {
+      for (int l = 0; l < 32; ++l) {
+        float a = lp[l];
+        for (int i = 0; i < R; ++i) a = fmaf(-beta[i], ly[l][i], a);
+        v[l] = a;
+      }
+      float sq[32];
+      for (int l = 0; l < 32; ++l) sq[l] = v[l] * v[l];
+      out[0] = (double)butterfly(v); out[1] = (double)butterfly(sq); out[2] = (double)cnt;
+      continue;
+    }
+    for (int l = 0; l < 32; ++l) { v[l] = lp[l]; }
+    out[0] = (double)butterfly(v);
+    for (int l = 0; l < 32; ++l) v[l] = lp[l] * lp[l];
+    out[1] = (double)butterfly(v);
+    out[2] = (double)cnt;
+    for (int i = 0; i < R; ++i) {
+      for (int l = 0; l < 32; ++l) v[l] = ly[l][i];
+      out[3 + i] = (double)butterfly(v);
+    }
+    int q = 3 + R;
+    for (int i = 0; i < R; ++i)
+      for (int j = i; j < R; ++j) {
+        for (int l = 0; l < 32; ++l) v[l] = ly[l][i] * ly[l][j];
+        out[q++] = (double)butterfly(v);
+      }
+    for (int i = 0; i < R; ++i) {
+      for (int l = 0; l < 32; ++l) v[l] = lp[l] * ly[l][i];
+      out[q + i] = (double)butterfly(v);
+    }
+  }
+}
+
+/* The server's accumulation of one phase: slices of slice_chunks chunks (the
+ * last one shorter), each reduced as its reduction CTA does it — thread t of
+ * 256 sums chunks t, t + 256, ... in order, then a halving tree — and added
+ * to the phase's running sums (starting at 0) slice after slice. */
+void oracle_serve_slices(const double* rows, int64_t nchunks, int W, int64_t slice_chunks, double* acc) {
+  static double sh[256];
+  for (int w = 0; w < W; ++w) acc[w] = 0.0;
+  for (int64_t s0 = 0; s0 < nchunks; s0 += slice_chunks) {
+    const int64_t cnt = nchunks - s0 < slice_chunks ? nchunks - s0 : slice_chunks;
+    for (int w = 0; w < W; ++w) {
+      for (int t = 0; t < 256; ++t) {
+        double a = 0.0;
+        for (int64_t c = t; c < cnt; c += 256) a += rows[(size_t)(s0 + c) * W + w];
+        sh[t] = a;
+      }
+      for (int o = 128; o > 0; o >>= 1)
+        for (int t = 0; t < o; ++t) sh[t] += sh[t + o];
+      acc[w] += sh[0];
+    }
+  }
 }
 
 /* ------------------------------------------------------------- MLMC ----- */
@@ -609,7 +919,7 @@ static void* job_run(void* arg) {
       j->s += y; j->s2 += (double)y * y; j->f += f; j->f2 += (double)f * f;
       if (j->payoffs) j->payoffs[p] = y;
     } else {
-      if (run_path(I, &d, j->exact, j->cap, NULL, NULL, NULL, NULL, NULL, x) < 0) j->bad = 1;
+      if (run_path(I, &d, j->exact, j->cap, NULL, NULL, NULL, NULL, NULL, x, NULL) < 0) j->bad = 1;
       float P = oracle_payoff(I, x) * I->discount;
       j->s += P; j->s2 += (double)P * P;
       if (j->payoffs) j->payoffs[p] = P;

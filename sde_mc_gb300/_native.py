@@ -60,6 +60,14 @@ class SdemcInst(ctypes.Structure):
         return ctypes.string_at(ctypes.byref(self), ctypes.sizeof(SdemcInst))
 
 
+class SdemcCvWeights(ctypes.Structure):
+    """Mirror of ``sdemc_cv_weights``: the served control variate's weight parameters."""
+    _fields_ = [("comp", _f8), ("inv_comp", _f8), ("scale_over_k", ctypes.c_float), ("inv_sig", ctypes.c_float),
+                ("drift", ctypes.c_float), ("T", ctypes.c_float), ("comp_j2", ctypes.c_float),
+                ("inv_comp_j2", ctypes.c_float), ("agg", ctypes.c_int32), ("wkind", ctypes.c_int32),
+                ("jumps", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
 class SdemcCfg(ctypes.Structure):
     _fields_ = [("block_threads", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32),
                 ("interleave", ctypes.c_int32), ("flags", ctypes.c_int32),
@@ -106,6 +114,8 @@ _PROTOS = {
     "sdemc_mlmc_terminals": (_I, [_P, _I, _I, ctypes.c_float, ctypes.c_float, _P, _P, _P, _P]),
     "sdemc_mlmc_replay": (_I, [_P, _I, _I, ctypes.c_float, ctypes.c_float, _I, _I, _I, _I, _P, _P,
                                _P, _P, _P, _P, _P, _P]),
+    "sdemc_serve_cv_weights": (_I, [_P, _P]),
+    "sdemc_serve_cv_paths": (_I, [_P, _I, _P, _P, _P, _P, _P, _P, _I, _P, _I, _P, _P]),
     "sdemc_server_create": (_I, [_P, ctypes.POINTER(_P)]),
     "sdemc_server_admit": (_I, [_P, _P]),
     "sdemc_server_poll": (_I, [_P, _P, _I, ctypes.POINTER(_I), ctypes.c_int64]),

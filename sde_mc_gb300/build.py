@@ -17,7 +17,9 @@ LIBDIR = os.path.join(HERE, "lib")
 OBJDIR = os.path.join(HERE, "_build")
 LIBNAME = "libsdemc.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
+# -ffp-contract=off: the host code's double arithmetic (the server's regression,
+# the control-variate weights) rounds every operation, on x86 and Arm alike.
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
               "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 
 

@@ -1,6 +1,8 @@
 // k_serve_cv.cu — K9 class kernels of the linear control variate (pilot
 // statistics and main run; diagonal noise, terminal payoff), the slot
-// install kernel and the per-slot reduction.
+// install kernel, the per-slot reduction, and the per-path view of the
+// control variate (sdemc_serve_cv_paths) that exports what the class kernels
+// compute path by path.
 #include "serve_kernels.cuh"
 
 namespace sdemc {
@@ -103,4 +105,127 @@ int launch_serve_reduce(ServeSlot* slots, const ServeEntry* entries, int n, cons
   return check_cuda(cudaGetLastError(), "serve_reduce_kernel launch");
 }
 
+// The per-path view: DeltaCvSink exactly as the class kernels run it, plus
+// exports of the raw normals of the path's own steps and of the weights
+// (w, g) evaluated at the start of each of its 4-step blocks.  A lane whose
+// path has reached T (frozen by the warp's lock-step) records nothing.
+template <int D>
+struct CvTraceSink {
+  static constexpr bool kWantsLeft = false;
+  DeltaCvSink<D> cv;
+  float* z;     // (S, D) of this path, or null
+  float* wg;    // (wcap, 2) of this path, or null
+  int S, wcap;
+  float T;
+  bool trunc;
+
+  SDEMC_DI void record(int b) {
+    if (!wg) return;
+    if (b < wcap) {
+      wg[2 * b] = cv.w;
+      wg[2 * b + 1] = cv.g;
+    } else {
+      trunc = true;
+    }
+  }
+  template <int DD> SDEMC_DI void init(const float* x) {
+    cv.template init<DD>(x);
+    record(0);
+  }
+  template <int DD, int NW>
+  SDEMC_DI void step(int k, const float* xl, const float* x, float t, float J, int sel, const float* dW,
+                     const float* dW2, const float* zr, int jump_one) {
+    const bool live = cv.tp < T;  // the step started before T
+    cv.template step<DD, NW>(k, xl, x, t, J, sel, dW, dW2, zr, jump_one);
+    if (!live) return;
+    if (k > 0 && (k & (kWeightEvery - 1)) == 0) record(k / kWeightEvery);
+    if (z) {
+      if (k < S) {
+#pragma unroll
+        for (int j = 0; j < D; ++j) z[(size_t)k * D + j] = zr[j];
+      } else {
+        trunc = true;
+      }
+    }
+  }
+  template <int DD, int NW> SDEMC_DI void finish(int, const float*, float) {}
+};
+
+template <int D>
+__global__ void __launch_bounds__(128)
+serve_cv_paths_kernel(const __grid_constant__ sdemc_inst I, const __grid_constant__ CvWeights cw, int S,
+                      float* d_pay, float* d_reg, float* zout, float* jt, float* jm, int32_t* jsel, int jcap,
+                      float* wg, int wcap, int32_t* status, int max_iters) {
+  constexpr int R = 2 * D + 1;
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = p < I.num_paths;
+  NativeDraws<D, SDEMC_NOISE_DIAG, SeedKeys> dr;
+  dr.init(I, (uint64_t)p, SeedKeys{(uint32_t)I.seed, (uint32_t)(I.seed >> 32)});
+  CvTraceSink<D> sk;
+  sk.cv.cw = &cw;
+  sk.z = (valid && zout) ? zout + (size_t)p * S * D : nullptr;
+  sk.wg = (valid && wg) ? wg + (size_t)p * wcap * 2 : nullptr;
+  sk.S = S;
+  sk.wcap = wcap;
+  sk.T = I.T;
+  sk.trunc = false;
+  bool ovf = false;
+  float x[D];
+  simulate<D, SDEMC_NOISE_DIAG, 0>(I, dr, sk, x, max_iters, ovf);
+  if (!valid) return;
+  d_pay[p] = __fmul_rn(payoff<D>(I, x), I.discount);
+#pragma unroll
+  for (int q = 0; q < R; ++q) d_reg[(size_t)p * R + q] = sk.cv.reg(q);
+  if (ovf || sk.trunc) atomicOr(status, SDEMC_EOVERFLOW);
+  // the path's jump stream (blocks 0, 1, 2, ...), times accumulated as the loop does
+  if (jcap > 0 && (jt || jm || jsel)) {
+    float nj = inf_f();
+    for (int j = 0; j < jcap; ++j) {
+      JumpDraw d{0.f, 0.f, 0};
+      if (I.rate > 0.f) {
+        d = jump_from_block<D>(I, dr.ps.block(kTagJumps, (uint32_t)j));
+        nj = j == 0 ? d.gap : __fadd_rn(nj, d.gap);
+      }
+      if (jt) jt[(size_t)p * jcap + j] = nj;
+      if (jm) jm[(size_t)p * jcap + j] = d.mark;
+      if (jsel) jsel[(size_t)p * jcap + j] = d.sel;
+    }
+  }
+}
+
 }  // namespace sdemc
+
+using namespace sdemc;
+
+extern "C" int sdemc_serve_cv_weights(const sdemc_inst* h_inst, sdemc_cv_weights* h_out) {
+  int rc = validate_inst(h_inst);
+  if (rc) return rc;
+  if (!h_out) return fail(SDEMC_EINVAL, "null weights output");
+  *h_out = serve_cv_weights(*h_inst);
+  return SDEMC_OK;
+}
+
+extern "C" int sdemc_serve_cv_paths(const sdemc_inst* h_inst, int steps_cap, float* d_payoff, float* d_reg,
+                                    float* d_z, float* d_jt, float* d_jm, int32_t* d_jsel, int jcap, float* d_wg,
+                                    int wcap, int32_t* d_status, void* stream) {
+  int rc = validate_inst(h_inst);
+  if (rc) return rc;
+  const sdemc_inst& I = *h_inst;
+  if (I.noise != SDEMC_NOISE_DIAG || (I.flags & SDEMC_INST_PAYOFF_AT_NOMINAL_STEP))
+    return fail(SDEMC_EUNSUPPORTED, "the served control variate needs diagonal noise and the terminal payoff");
+  if (!d_payoff || !d_reg || !d_status) return fail(SDEMC_EINVAL, "null payoff, regressor or status buffer");
+  if (d_z && steps_cap < 1) return fail(SDEMC_EINVAL, "steps_cap %d < 1 with normals exported", steps_cap);
+  if (d_wg && wcap < 1) return fail(SDEMC_EINVAL, "wcap %d < 1 with weights exported", wcap);
+  if ((d_jt || d_jm || d_jsel) && jcap < 1) return fail(SDEMC_EINVAL, "jcap %d < 1 with jumps exported", jcap);
+  if (I.num_paths == 0) return SDEMC_OK;
+  const CvWeights cw = serve_cv_weights(I);
+  const unsigned blocks = (unsigned)((I.num_paths + 127) / 128);
+  cudaStream_t s = (cudaStream_t)stream;
+  const int mi = max_iterations(&I);
+#define SDEMC_CVP_CASE(D_, N_)                                                                              \
+  serve_cv_paths_kernel<D_><<<blocks, 128, 0, s>>>(I, cw, steps_cap, d_payoff, d_reg, d_z, d_jt, d_jm, d_jsel, \
+                                                   jcap, d_wg, wcap, d_status, mi);
+  SDEMC_DISPATCH_DIM(SDEMC_NOISE_DIAG, I.dim, SDEMC_CVP_CASE)
+#undef SDEMC_CVP_CASE
+  return check_cuda(cudaGetLastError(), "serve_cv_paths_kernel launch");
+}

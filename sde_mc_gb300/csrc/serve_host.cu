@@ -65,73 +65,6 @@ double path_cost(const sdemc_inst& I) {
   return steps * (double)I.dim;
 }
 
-// The control variate's integrand weight for a descriptor (see CvWeights):
-// a Black-Scholes call (or put) delta of the payoff's underlying with the
-// lognormal volatility of that underlying, jumps included.  Any choice keeps
-// the estimator unbiased; a good one makes the variance reduction large.
-CvWeights cv_weights(const sdemc_inst& I) {
-  CvWeights cw{};
-  const int d = I.dim;
-  double jump_var = 0.0;
-  const double a = I.mark_p[0], g = I.mark_p[1];
-  const double kappa = std::exp(a + 0.5 * g * g) - 1.0;
-  // the jump regressor is carried divided by its compensator rate, so it
-  // needs E[J] != 0; an asset that never jumps gets rate 0 (regressor 0)
-  if (I.rate > 0.f && I.mark == SDEMC_MARK_LOGNORMAL && std::fabs(kappa) > 1e-9) {
-    for (int i = 0; i < d; ++i) {
-      double p = 1.0;
-      if (I.jump_target == SDEMC_JUMP_ONE_ASSET) {
-        const double lo = i > 0 ? I.jump_cdf[i - 1] : 0.0, hi = i < d - 1 ? I.jump_cdf[i] : 1.0;
-        p = hi - lo;
-      }
-      cw.comp[i] = (float)((double)I.rate * p * kappa);
-    }
-    cw.jumps = 1;
-    // E[J^2] for J = exp(N(a, g^2)) - 1
-    cw.comp_j2 = (float)((double)I.rate * (std::exp(2.0 * a + 2.0 * g * g) - 2.0 * std::exp(a + 0.5 * g * g) + 1.0));
-    jump_var = (double)I.rate * (a * a + g * g) / (I.jump_target == SDEMC_JUMP_ONE_ASSET ? d : 1);
-  }
-  switch (I.payoff) {
-    case SDEMC_PAYOFF_EUROCALL: cw.wkind = 1; cw.agg = 0; break;
-    case SDEMC_PAYOFF_EUROPUT: cw.wkind = 2; cw.agg = 0; break;
-    case SDEMC_PAYOFF_BASKET_ARITH:
-    case SDEMC_PAYOFF_BASKET_GEO: cw.wkind = 1; cw.agg = 1; break;
-    case SDEMC_PAYOFF_RAINBOW:
-    case SDEMC_PAYOFF_BESTOF: cw.wkind = 1; cw.agg = 2; break;
-    default: cw.wkind = 0; break;
-  }
-  if (I.payoff_log || !(I.strike > 0.f)) cw.wkind = 0;
-  // correlation from the packed Cholesky rows, then the underlying's variance
-  double L[SDEMC_MAX_DIM][SDEMC_MAX_DIM] = {};
-  for (int i = 0, q = 0; i < d; ++i)
-    for (int j = 0; j <= i; ++j) L[i][j] = I.chol[q++];
-  double sig[SDEMC_MAX_DIM];
-  for (int i = 0; i < d; ++i) sig[i] = std::fabs((double)I.diff_q[i]);
-  // Heston's price volatility is sqrt(v): weight with the initial variance's
-  if (I.model == SDEMC_MODEL_HESTON) sig[0] = std::sqrt(std::max((double)I.x0[1], 0.0));
-  double var = 0.0;
-  if (cw.agg == 0) {
-    var = sig[0] * sig[0];
-  } else if (cw.agg == 1) {
-    for (int i = 0; i < d; ++i)
-      for (int j = 0; j < d; ++j) {
-        double c = 0.0;
-        for (int k = 0; k < d; ++k) c += L[i][k] * L[j][k];
-        var += sig[i] * sig[j] * c;
-      }
-    var /= (double)d * d;
-  } else {
-    for (int i = 0; i < d; ++i) var += sig[i] * sig[i];
-    var /= d;
-  }
-  var = std::max(var + jump_var, 1e-8);
-  cw.inv_sig = (float)(1.0 / std::sqrt(var));
-  cw.drift = (float)((double)I.disc_rate + 0.5 * var);
-  cw.T = I.T;
-  cw.scale_over_k = cw.wkind ? (float)((double)I.payoff_scale / (double)I.strike) : 1.f;
-  return cw;
-}
-
 // Solve C beta = c for a symmetric positive semi-definite C (d <= 16) by
 // Cholesky with a small diagonal jitter; returns false if C is degenerate.
 // A regressor that is identically zero gets a zero coefficient.
@@ -202,6 +135,76 @@ struct TickBuf {
 };
 
 }  // namespace
+
+// The control variate's integrand weight for a descriptor (see CvWeights):
+// a Black-Scholes call (or put) delta of the payoff's underlying with the
+// lognormal volatility of that underlying, jumps included.  Any choice keeps
+// the estimator unbiased; a good one makes the variance reduction large.
+CvWeights serve_cv_weights(const sdemc_inst& I) {
+  CvWeights cw{};
+  const int d = I.dim;
+  double jump_var = 0.0;
+  const double a = I.mark_p[0], g = I.mark_p[1];
+  const double kappa = std::exp(a + 0.5 * g * g) - 1.0;
+  // the jump regressor is carried divided by its compensator rate, so it
+  // needs E[J] != 0; an asset that never jumps gets rate 0 (regressor 0)
+  if (I.rate > 0.f && I.mark == SDEMC_MARK_LOGNORMAL && std::fabs(kappa) > 1e-9) {
+    for (int i = 0; i < d; ++i) {
+      double p = 1.0;
+      if (I.jump_target == SDEMC_JUMP_ONE_ASSET) {
+        const double lo = i > 0 ? I.jump_cdf[i - 1] : 0.0, hi = i < d - 1 ? I.jump_cdf[i] : 1.0;
+        p = hi - lo;
+      }
+      cw.comp[i] = (float)((double)I.rate * p * kappa);
+    }
+    cw.jumps = 1;
+    // E[J^2] for J = exp(N(a, g^2)) - 1
+    cw.comp_j2 = (float)((double)I.rate * (std::exp(2.0 * a + 2.0 * g * g) - 2.0 * std::exp(a + 0.5 * g * g) + 1.0));
+    jump_var = (double)I.rate * (a * a + g * g) / (I.jump_target == SDEMC_JUMP_ONE_ASSET ? d : 1);
+  }
+  switch (I.payoff) {
+    case SDEMC_PAYOFF_EUROCALL: cw.wkind = 1; cw.agg = 0; break;
+    case SDEMC_PAYOFF_EUROPUT: cw.wkind = 2; cw.agg = 0; break;
+    case SDEMC_PAYOFF_BASKET_ARITH:
+    case SDEMC_PAYOFF_BASKET_GEO: cw.wkind = 1; cw.agg = 1; break;
+    case SDEMC_PAYOFF_RAINBOW:
+    case SDEMC_PAYOFF_BESTOF: cw.wkind = 1; cw.agg = 2; break;
+    default: cw.wkind = 0; break;
+  }
+  if (I.payoff_log || !(I.strike > 0.f)) cw.wkind = 0;
+  // correlation from the packed Cholesky rows, then the underlying's variance
+  double L[SDEMC_MAX_DIM][SDEMC_MAX_DIM] = {};
+  for (int i = 0, q = 0; i < d; ++i)
+    for (int j = 0; j <= i; ++j) L[i][j] = I.chol[q++];
+  double sig[SDEMC_MAX_DIM];
+  for (int i = 0; i < d; ++i) sig[i] = std::fabs((double)I.diff_q[i]);
+  // Heston's price volatility is sqrt(v): weight with the initial variance's
+  if (I.model == SDEMC_MODEL_HESTON) sig[0] = std::sqrt(std::max((double)I.x0[1], 0.0));
+  double var = 0.0;
+  if (cw.agg == 0) {
+    var = sig[0] * sig[0];
+  } else if (cw.agg == 1) {
+    for (int i = 0; i < d; ++i)
+      for (int j = 0; j < d; ++j) {
+        double c = 0.0;
+        for (int k = 0; k < d; ++k) c += L[i][k] * L[j][k];
+        var += sig[i] * sig[j] * c;
+      }
+    var /= (double)d * d;
+  } else {
+    for (int i = 0; i < d; ++i) var += sig[i] * sig[i];
+    var /= d;
+  }
+  var = std::max(var + jump_var, 1e-8);
+  cw.inv_sig = (float)(1.0 / std::sqrt(var));
+  cw.drift = (float)((double)I.disc_rate + 0.5 * var);
+  cw.T = I.T;
+  cw.scale_over_k = cw.wkind ? (float)((double)I.payoff_scale / (double)I.strike) : 1.f;
+  for (int i = 0; i < SDEMC_MAX_DIM; ++i)
+    cw.inv_comp[i] = cw.comp[i] != 0.f ? (float)(1.0 / (double)cw.comp[i]) : 0.f;
+  cw.inv_comp_j2 = cw.comp_j2 != 0.f ? (float)(1.0 / (double)cw.comp_j2) : 0.f;
+  return cw;
+}
 
 struct Server {
   sdemc_server_cfg cfg{};
@@ -367,7 +370,7 @@ void Server::admit_locked() {
     in.rec.st.phase = 0;
     in.rec.st.width = h.width;
     in.rec.st.kind = h.kind;
-    h.cw = cv_weights(I);
+    h.cw = serve_cv_weights(I);
     in.rec.st.cw = h.cw;
     staged.push_back(in);
     pending.pop_front();

@@ -37,23 +37,21 @@ SDEMC_HDI int pilot_width(int d) {
 }
 SDEMC_HDI int kind_width(int kind, int d) { return kind == kKindPilotStats ? pilot_width(d) : 3; }
 
-// Integrand weights of the control variate: w(t, X) = N(d1) (call-like
-// payoffs) or N(d1) - 1 (puts) of a lognormal proxy of the payoff's
-// underlying A = payoff_scale * agg(X) (asset 0, mean or max): d1 =
-// (ln(A/K) + drift tau) / (sig sqrt(tau)), tau = T - t; w = 1 when
-// wkind == 0 — a delta; and g(t, X) = (A/K) phi(d1) / (sig sqrt(tau)) (g = 1
-// when wkind == 0) — a gamma scaled by A^2/K.  Any deterministic weights keep
-// the control variate unbiased; these make it close to a delta hedge plus the
-// second-order jump exposure.  comp[i] is the jump compensator rate
-// lambda_i E[J] of asset i and comp_j2 = lambda E[J^2]; jump regressors are on
-// only when those rates are known exactly (lognormal marks).
-struct CvWeights {
-  float comp[SDEMC_MAX_DIM];
-  float scale_over_k;  // payoff_scale / K
-  float inv_sig, drift, T;
-  float comp_j2;
-  int32_t agg, wkind, jumps;
-};
+// Integrand weights of the control variate (sdemc_cv_weights in the header):
+// w(t, X) = N(d1) (call-like payoffs) or N(d1) - 1 (puts) of a lognormal
+// proxy of the payoff's underlying A = payoff_scale * agg(X) (asset 0, mean
+// or max): d1 = (ln(A/K) + drift tau) / (sig sqrt(tau)), tau = T - t; w = 1
+// when wkind == 0 — a delta; and g(t, X) = (A/K) phi(d1) / (sig sqrt(tau))
+// (g = 1 when wkind == 0) — a gamma scaled by A^2/K.  Any deterministic
+// weights keep the control variate unbiased; these make it close to a delta
+// hedge plus the second-order jump exposure.  comp[i] is the jump
+// compensator rate lambda_i E[J] of asset i and comp_j2 = lambda E[J^2]
+// (inv_comp, inv_comp_j2 their reciprocals); jump regressors are on only when
+// those rates are known exactly (lognormal marks).
+using CvWeights = sdemc_cv_weights;
+
+// The weights the server derives for a descriptor at admission (host).
+CvWeights serve_cv_weights(const sdemc_inst& I);
 
 struct ServeState {
   int64_t cursor;              // next local path index (the request's RNG counter)
@@ -114,8 +112,9 @@ struct ServeParams {
 // compensators on the jump-adapted grid), so each has mean exactly zero under
 // the Euler scheme whatever the weights.  Frozen lanes (dt = 0, dW = 0, no
 // jump) add nothing.  A jump regressor is carried as a with r = -comp a:
-// every step adds weight x dt, a jump subtracts weight x J / comp (the
-// compensator rates are nonzero whenever jumps are on).
+// every step adds weight x dt, a jump subtracts weight x J x (1 / comp) (the
+// compensator rates are nonzero whenever jumps are on; the reciprocals are
+// rounded once, on the host).
 constexpr int kWeightEvery = 4;
 
 template <int D>
@@ -172,8 +171,8 @@ struct DeltaCvSink {
       if (J != 0.f) {
 #pragma unroll
         for (int i = 0; i < D; ++i)
-          if (!jump_one || i == sel) a[i] = __fmaf_rn(-__fmul_rn(w, xp[i]), __fdividef(J, cw->comp[i]), a[i]);
-        ag = __fmaf_rn(-g, __fdividef(__fmul_rn(J, J), cw->comp_j2), ag);
+          if (!jump_one || i == sel) a[i] = __fmaf_rn(-__fmul_rn(w, xp[i]), __fmul_rn(J, cw->inv_comp[i]), a[i]);
+        ag = __fmaf_rn(-g, __fmul_rn(__fmul_rn(J, J), cw->inv_comp_j2), ag);
       }
     }
 #pragma unroll

@@ -129,6 +129,42 @@ def materialise(inst, steps_cap, want=("paths", "left", "time", "jumps", "normal
     return out
 
 
+def serve_cv_weights(inst):
+    """The served control variate's weight parameters for a descriptor (host only)."""
+    cw = N.SdemcCvWeights()
+    N.check(N.load().sdemc_serve_cv_weights(ctypes.byref(inst), ctypes.byref(cw)), "sdemc_serve_cv_weights")
+    return cw
+
+
+def serve_cv_paths(inst, steps_cap=0, jcap=0, wcap=0, device=None):
+    """The served control variate path by path: each path's discounted payoff
+    'payoff' (n) and its 2d + 1 regressors 'reg' (n, 2d + 1), exactly as the
+    server's kernels compute them.  steps_cap > 0 also exports the raw normals
+    'z' (n, steps_cap, d); jcap > 0 the jump stream 'jt', 'jm', 'jsel'; wcap > 0
+    the weights 'wg' (n, wcap, 2) of every 4-step block.  Plus 'status'."""
+    dev = _dev(device)
+    n, d = int(inst.num_paths), int(inst.dim)
+    f32 = dict(dtype=torch.float32, device=dev)
+    out = {"payoff": torch.empty(n, **f32), "reg": torch.empty((n, 2 * d + 1), **f32)}
+    if steps_cap > 0:
+        out["z"] = torch.zeros((n, steps_cap, d), **f32)
+    if jcap > 0:
+        out["jt"] = torch.empty((n, jcap), **f32)
+        out["jm"] = torch.empty((n, jcap), **f32)
+        out["jsel"] = torch.empty((n, jcap), dtype=torch.int32, device=dev)
+    if wcap > 0:
+        out["wg"] = torch.zeros((n, wcap, 2), **f32)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    g = out.get
+    rc = N.load().sdemc_serve_cv_paths(
+        ctypes.byref(inst), int(steps_cap), N.ptr(out["payoff"]), N.ptr(out["reg"]), N.ptr(g("z")),
+        N.ptr(g("jt")), N.ptr(g("jm")), N.ptr(g("jsel")), int(jcap), N.ptr(g("wg")), int(wcap), N.ptr(status),
+        N.stream_handle(dev))
+    N.check(rc, "sdemc_serve_cv_paths")
+    out["status"] = status
+    return out
+
+
 def replay(inst, dw, jump_times=None, marks=None, asset=None, device=None):
     """K3: replay recorded draws.  dw (bs, S, d[, 2]); jump_times (bs, MJ);
     marks/asset (bs, S).  Returns dict of paths/left/time/jumps/payoffs/steps/status."""

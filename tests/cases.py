@@ -99,3 +99,25 @@ def inst_for(case, num_paths=0, seed=7, path_offset=0, steps=None):
 def zdim(inst):
     d = inst.dim
     return d if inst.noise == N.NOISE_DIAG else (d + 1 if inst.noise == N.NOISE_INDEP_SHARED else 2 * d)
+
+
+def served_cv_cases():
+    """Requests for the served control variate's parity tests: dimensions 1, 2,
+    6 and 8, common and per-asset jumps, call, put, digital, rainbow and
+    basket payoffs (every weight kind and aggregate the server uses)."""
+    def merton(d, sig, rate, steps, payoff, strike=1.0):
+        corr = sm.get_corr_matrix([0.3] * (d * (d - 1) // 2)) if d > 1 else None
+        m = sm.Merton(0.02, torch.tensor(sig), rate, -0.1, 0.2, torch.ones(d), dim=d, corr_matrix=corr)
+        return sm.JumpEulerSolver(m, 1.0, steps), payoff(strike), sm.ConstantShortRate(0.02)
+
+    return {
+        "call1d": merton(1, [0.2], 2.0, 50, sm.EuroCall),
+        "put1d": merton(1, [0.25], 1.5, 40, sm.EuroPut),
+        "digital1d": merton(1, [0.2], 2.0, 40, sm.Digital),
+        "rainbow2d_per_asset": indep2d(64),
+        "basket6": merton(6, [0.15, 0.2, 0.25, 0.3, 0.35, 0.4], 2.0, 48, sm.Basket, 1.05),
+        "basket8": merton(8, [0.1 + 0.04 * i for i in range(8)], 1.0, 32, sm.Basket, 0.95),
+        "bestof3_uniform": (sm.EulerSolver(sm.Gbm(0.02, torch.tensor([0.2, 0.25, 0.3]), torch.ones(3), 3,
+                                                  corr_matrix=sm.get_corr_matrix([0.3] * 3)), 1.0, 24),
+                            sm.BestOf(1.1), sm.ConstantShortRate(0.02)),
+    }
