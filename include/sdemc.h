@@ -366,6 +366,31 @@ int sdemc_mlmc_replay(const sdemc_inst* h_inst, int fine, int coarse,
                       const int32_t* d_asset, float* d_xf, float* d_xc,
                       int32_t* d_status, void* stream);
 
+/* Every column multilevel_solve returns, for num_paths coupled paths with the
+ * Philox draws of sdemc_mlmc_level.  Jump-adapted grid
+ * (JumpDiffusionSolver.multilevel_solve, sde_mc/solvers.py:228-307): d_paths_fine
+ * and d_paths_coarse (n, cols, dim) hold the initial state and the fine and
+ * coarse states after each coarse step (cols_fine == cols_coarse = the
+ * reference's storage, coarse + max_jumps + 1); a path keeps its final state in
+ * the columns after its own last step, as the reference's batch loop leaves
+ * it, and d_steps (n, nullable) receives its own coarse steps, so the
+ * reference's total_steps_coarse is their maximum.  Uniform grid
+ * (DiffusionSolver.multilevel_solve, :90-119): d_paths_fine (n, fine + 1, dim),
+ * d_paths_coarse (n, coarse + 1, dim) and, nullable, the fine increments
+ * d_normals (n, fine, dim[, 2]).  A path needing more columns sets
+ * SDEMC_EOVERFLOW in *d_status (the reference raises IndexError).           */
+int sdemc_mlmc_paths(const sdemc_inst* h_inst, int fine, int coarse, float h_fine, float h_coarse,
+                     int cols_fine, int cols_coarse, float* d_paths_fine, float* d_paths_coarse,
+                     float* d_normals, int32_t* d_steps, int32_t* d_status, void* stream);
+
+/* sdemc_mlmc_replay with the columns of sdemc_mlmc_paths as well.         */
+int sdemc_mlmc_replay_paths(const sdemc_inst* h_inst, int fine, int coarse, float h_fine,
+                            float h_coarse, int bs, int fine_cap, int coarse_cap, int max_jumps,
+                            const float* d_jump_times, const float* d_dw, const float* d_marks,
+                            const int32_t* d_asset, int cols_fine, int cols_coarse,
+                            float* d_paths_fine, float* d_paths_coarse, float* d_xf, float* d_xc,
+                            int32_t* d_steps, int32_t* d_status, void* stream);
+
 /* ---- K5/K6: learned control variate -------------------------------------
  * The integrand network of the adapted control variate, the reference's
  * Mlp(1+d, [64, 64, 64], d) with ReLU and no batch norm (sde_mc/nets.py:39-93),

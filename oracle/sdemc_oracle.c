@@ -413,12 +413,13 @@ static void cv_weights_block(cvacc_t* c, int b) {
   /* The kernel evaluates ln, 1/sqrt, the normal cdf and exp with CUDA's
    * intrinsics (absolute error of __logf <= 2^-21.41 near 1, otherwise 3 ulp;
    * rsqrtf 2 ulp; normcdff 5 ulp; __expf 2 + 1.173|x| ulp); propagate those
-   * through d1 = (ln m + drift tau) is, w = N(d1), g = m is phi(d1), with a
-   * factor 2 to spare. */
+   * through d1 = (ln m + drift tau) is, w = N(d1) (or N(d1) - 1), g = m is
+   * phi(d1), with a factor 2 to spare. */
   const double ulp = 1.0 / 8388608.0;
   const double dd1 = fabs((double)is) * (4.0e-7 + 8.0 * ulp * fabs((double)lm)) + fabs((double)d1) * 8.0 * ulp;
   const double phi = 0.3989422804014327 * exp(-0.5 * (double)d1 * d1);
-  const double bw = 2.0 * (phi * dd1 + 8.0 * ulp * fabs((double)v)) + 1e-12;
+  /* a put's weight N(d1) - 1 rounds once more on each side: half an ulp of |w| each */
+  const double bw = 2.0 * (phi * dd1 + 8.0 * ulp * fabs((double)v) + ulp * fabs((double)w)) + 1e-12;
   const double x = 0.5 * (double)d1 * d1;
   const double bg = 2.0 * fabs((double)g) * (8.0 * ulp + fabs((double)d1) * dd1 + (8.0 + 1.2 * x) * ulp) + 1e-12;
   const double ew = fabs((double)rw - (double)w) / bw, eg = fabs((double)rg - (double)g) / bg;

@@ -114,6 +114,9 @@ _PROTOS = {
     "sdemc_mlmc_terminals": (_I, [_P, _I, _I, ctypes.c_float, ctypes.c_float, _P, _P, _P, _P]),
     "sdemc_mlmc_replay": (_I, [_P, _I, _I, ctypes.c_float, ctypes.c_float, _I, _I, _I, _I, _P, _P,
                                _P, _P, _P, _P, _P, _P]),
+    "sdemc_mlmc_paths": (_I, [_P, _I, _I, ctypes.c_float, ctypes.c_float, _I, _I, _P, _P, _P, _P, _P, _P]),
+    "sdemc_mlmc_replay_paths": (_I, [_P, _I, _I, ctypes.c_float, ctypes.c_float, _I, _I, _I, _I, _P, _P, _P,
+                                     _P, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
     "sdemc_serve_cv_weights": (_I, [_P, _P]),
     "sdemc_serve_cv_paths": (_I, [_P, _I, _P, _P, _P, _P, _P, _P, _I, _P, _I, _P, _P]),
     "sdemc_server_create": (_I, [_P, ctypes.POINTER(_P)]),

@@ -189,8 +189,33 @@ def replay(inst, dw, jump_times=None, marks=None, asset=None, device=None):
     return out
 
 
+def mlmc_paths(inst, fine, coarse, h_fine, h_coarse, cols, normals=False, device=None):
+    """K2 with every column multilevel_solve returns: dict of 'paths_fine',
+    'paths_coarse', 'steps' (own coarse steps per path), 'status' and, on the
+    uniform grid with normals=True, the fine increments 'normals'.  cols =
+    (fine columns, coarse columns)."""
+    dev = _dev(device)
+    n, d = int(inst.num_paths), int(inst.dim)
+    cf, cc = int(cols[0]), int(cols[1])
+    f32 = dict(dtype=torch.float32, device=dev)
+    out = {"paths_fine": torch.empty((n, cf, d), **f32), "paths_coarse": torch.empty((n, cc, d), **f32),
+           "steps": torch.zeros(n, dtype=torch.int32, device=dev)}
+    if normals and inst.grid == N.GRID_UNIFORM:
+        nw = 1 if inst.noise == N.NOISE_DIAG else 2
+        out["normals"] = torch.empty((n, int(fine), d) if nw == 1 else (n, int(fine), d, 2), **f32)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    rc = N.load().sdemc_mlmc_paths(ctypes.byref(inst), int(fine), int(coarse), float(h_fine), float(h_coarse), cf, cc,
+                                   N.ptr(out["paths_fine"]), N.ptr(out["paths_coarse"]), N.ptr(out.get("normals")),
+                                   N.ptr(out["steps"]), N.ptr(status), N.stream_handle(dev))
+    N.check(rc, "sdemc_mlmc_paths")
+    out["status"] = status
+    return out
+
+
 def mlmc_replay(inst, fine, coarse, h_fine, h_coarse, dw, coarse_cap, jump_times=None, marks=None,
-                asset=None, device=None):
+                asset=None, device=None, cols=None):
+    """K2 on recorded draws: terminal states 'xf', 'xc' (and with cols = (fine
+    columns, coarse columns) also 'paths_fine', 'paths_coarse', 'steps')."""
     dev = _dev(device)
     bs, Sf = int(dw.shape[0]), int(dw.shape[1])
     d = int(inst.dim)
@@ -202,6 +227,18 @@ def mlmc_replay(inst, fine, coarse, h_fine, h_coarse, dw, coarse_cap, jump_times
     xc = torch.empty((bs, d), dtype=torch.float32, device=dev)
     status = torch.zeros(1, dtype=torch.int32, device=dev)
     mj = int(jump_times.shape[1]) if jump_times is not None else 0
+    if cols is not None:
+        cf, cc = int(cols[0]), int(cols[1])
+        pf = torch.empty((bs, cf, d), dtype=torch.float32, device=dev)
+        pc = torch.empty((bs, cc, d), dtype=torch.float32, device=dev)
+        steps = torch.zeros(bs, dtype=torch.int32, device=dev)
+        rc = N.load().sdemc_mlmc_replay_paths(ctypes.byref(inst), int(fine), int(coarse), float(h_fine),
+                                              float(h_coarse), bs, Sf, int(coarse_cap), mj, N.ptr(jump_times),
+                                              N.ptr(dw), N.ptr(marks), N.ptr(asset), cf, cc, N.ptr(pf), N.ptr(pc),
+                                              N.ptr(xf), N.ptr(xc), N.ptr(steps), N.ptr(status),
+                                              N.stream_handle(dev))
+        N.check(rc, "sdemc_mlmc_replay_paths")
+        return dict(xf=xf, xc=xc, paths_fine=pf, paths_coarse=pc, steps=steps, status=status)
     rc = N.load().sdemc_mlmc_replay(ctypes.byref(inst), int(fine), int(coarse), float(h_fine),
                                     float(h_coarse), bs, Sf, int(coarse_cap), mj, N.ptr(jump_times),
                                     N.ptr(dw), N.ptr(marks), N.ptr(asset), N.ptr(xf), N.ptr(xc),

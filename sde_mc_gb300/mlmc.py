@@ -60,15 +60,24 @@ def mc_multilevel(trials, levels, solver, payoff, discounter, bs=None):
     return MCStatistics(mean, sd, time.time() - start, trials[-1])
 
 
-def get_optimal_trials(trials, levels, epsilon, solver, payoff, discounter):
-    """Giles' allocation N_l = (1.96/eps)^2 sqrt(V_l h_l) sum_k sqrt(V_k / h_k)
-    from a pilot of ``trials`` paths per level."""
-    est = level_estimates([int(trials)] * len(levels), levels, solver, payoff, discounter)
-    var = torch.tensor([v for _, v in est], dtype=torch.float64)
-    h = solver.time_interval / torch.tensor(levels, dtype=torch.float64)
+def optimal_trials_from_variances(level_vars, levels, time_interval, epsilon):
+    """Giles' allocation N_l = (1.96/eps)^2 sqrt(V_l h_l) sum_k sqrt(V_k / h_k),
+    h_l = T / levels[l], in float32 exactly as the reference evaluates it
+    (sde_mc/mlmc.py:92-96), rounded up."""
+    var = torch.as_tensor(level_vars, dtype=torch.float64).to(torch.float32)
+    h = time_interval / torch.tensor(levels)
     total = (var / h).sqrt().sum()
     opt = (1.96 ** 2 / (epsilon * epsilon)) * (var * h).sqrt() * total
     return opt.ceil().long().tolist()
+
+
+def get_optimal_trials(trials, levels, epsilon, solver, payoff, discounter):
+    """Giles' allocation from a pilot of ``trials`` paths per level
+    (sde_mc/mlmc.py:77-97).  As the reference does, it leaves the solver's
+    num_steps at levels[0]."""
+    solver.num_steps = levels[0]
+    est = level_estimates([int(trials)] * len(levels), levels, solver, payoff, discounter)
+    return optimal_trials_from_variances([v for _, v in est], levels, solver.time_interval, epsilon)
 
 
 def mlmc_bs_from_trials(trials, levels, max_mem=5 * 10 ** 8, dim=1, max_jumps=0):

@@ -82,10 +82,16 @@ class DiffusionSolver(SdeSolver):
         return self._out(out["paths"]), self._out(out["normals"])
 
     def multilevel_solve(self, bs, levels, return_normals=False):
-        """Coupled fine/coarse paths; returns ((paths_fine, paths_coarse), None)
-        holding the initial and terminal columns (the only ones the estimators
-        read, sde_mc/mlmc.py:59-69)."""
-        return _multilevel_terminals(self, bs, levels)
+        """Coupled fine/coarse paths (sde_mc/solvers.py:90-119): ((paths_fine
+        (bs, fine + 1, dim), paths_coarse (bs, coarse + 1, dim)), the fine
+        increments (bs, fine, dim[, 2]))."""
+        bs = int(bs)
+        fine, coarse = int(levels[0]), int(levels[1])
+        inst = self.lower(num_paths=bs, num_steps=coarse)
+        hf, hc = level_steps(self, fine, coarse)
+        out = K.mlmc_paths(inst, fine, coarse, hf, hc, (fine + 1, coarse + 1), normals=True)
+        N.status_error(out["status"].item(), "multilevel_solve")
+        return (self._out(out["paths_fine"]), self._out(out["paths_coarse"])), self._out(out["normals"])
 
 
 class EulerSolver(EulerScheme, DiffusionSolver):
@@ -161,9 +167,24 @@ class JumpDiffusionSolver(SdeSolver):
                                   self._out(out["jumps"]))
 
     def multilevel_solve(self, bs, levels, return_normals=False):
-        """Coupled fine/coarse jump-adapted paths; returns ((paths_fine,
-        paths_coarse), None) holding the initial and terminal columns (the only
-        ones mc_multilevel and get_optimal_trials read)."""
+        """Coupled fine/coarse jump-adapted paths (sde_mc/solvers.py:228-307):
+        ((paths_fine, paths_coarse), None), each (bs, total_steps_coarse + 1,
+        dim) with the states after every coarse step (a finished path keeps its
+        final state).  The estimators (mc_multilevel, get_optimal_trials) read
+        only terminal states and run the level kernels directly."""
+        bs = int(bs)
+        fine, coarse = int(levels[0]), int(levels[1])
+        inst = self.lower(num_paths=bs, num_steps=coarse)
+        hf, hc = level_steps(self, fine, coarse)
+        cols = coarse + int(self.max_jumps) + 1
+        out = K.mlmc_paths(inst, fine, coarse, hf, hc, (cols, cols))
+        N.status_error(out["status"].item(), "multilevel_solve")
+        total = int(out["steps"].max().item()) if bs > 0 else 0
+        return (self._out(out["paths_fine"][:, :total + 1]), self._out(out["paths_coarse"][:, :total + 1])), None
+
+    def multilevel_terminals(self, bs, levels):
+        """((paths_fine, paths_coarse), None) with only the initial and terminal
+        columns of multilevel_solve (no column storage)."""
         return _multilevel_terminals(self, bs, levels)
 
 

@@ -34,6 +34,14 @@ def levy2d(steps=16, seed=1):
     return sm.JumpEulerSolver(sde, 1.0, steps, seed=seed), sm.Rainbow(1.0), sm.ConstantShortRate(0.02)
 
 
+def levy2d_exact(steps=4, seed=1):
+    """The LevyRainbowMLMC preset's model (sde_mc/problem.py:93-106): Levy
+    'indep', exact_jumps=True."""
+    lev = sm.ExpExampleLevy(1, 1, 0.5, 2, 0.02, 0.2, 0.2, 0.2, 2)
+    return (sm.JumpEulerSolver(sm.LevySde(lev, torch.ones(2)), 1.0, steps, exact_jumps=True, seed=seed),
+            sm.Rainbow(1.0), sm.ConstantShortRate(0.02))
+
+
 def gbm_uniform(steps=12, seed=1):
     g = sm.Gbm(0.02, torch.tensor([0.2, 0.25]), torch.tensor([1., 1.5]), 2, corr_matrix=sm.get_corr_matrix([-0.3]))
     return sm.EulerSolver(g, 1.0, steps, seed=seed), sm.EuroCall(1.0), sm.ConstantShortRate(0.02)

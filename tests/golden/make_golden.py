@@ -143,10 +143,14 @@ def jump_replay_case(sde_mc, torch, solver, bs, payoff, disc, seed, one_asset=Fa
         out['asset'] = k.numpy().astype(np.int32)
     else:
         out['marks'] = marks_full.numpy().astype(np.float32)
+    if full:
+        # every column multilevel_solve returns: (bs, total_steps_coarse + 1, dim) each
+        out['paths_fine'] = pf.numpy().astype(np.float32)
+        out['paths_coarse'] = pc.numpy().astype(np.float32)
     return out
 
 
-def mlmc_replay_case(sde_mc, torch, solver, bs, levels, seed, one_asset=False):
+def mlmc_replay_case(sde_mc, torch, solver, bs, levels, seed, one_asset=False, full=False):
     fine, coarse = levels
     factor = fine // coarse
     torch.manual_seed(seed)
@@ -173,6 +177,10 @@ def mlmc_replay_case(sde_mc, torch, solver, bs, levels, seed, one_asset=False):
         out['asset'] = k.numpy().astype(np.int32)
     else:
         out['marks'] = marks_full.numpy().astype(np.float32)
+    if full:
+        # every column multilevel_solve returns: (bs, total_steps_coarse + 1, dim) each
+        out['paths_fine'] = pf.numpy().astype(np.float32)
+        out['paths_coarse'] = pc.numpy().astype(np.float32)
     return out
 
 
@@ -335,11 +343,77 @@ def heston_asian_fixtures(sm, torch):
         np.savez_compressed(os.path.join(HERE, name + '.npz'), **{k: np.asarray(v) for k, v in arrs.items()})
 
 
+def mlmc_columns_fixture(sm, torch):
+    """Every column of the coupled paths multilevel_solve returns, with the
+    draws it used: JumpDiffusionSolver.multilevel_solve (sde_mc/solvers.py:
+    228-307; columns at each coarse step, to the batch's last) for a 1-D
+    Merton (common jumps) and the 2-D per-asset-jump model, and
+    DiffusionSolver.multilevel_solve (:90-119; every fine and every coarse
+    step, the normals it returns) for a correlated 2-D GBM."""
+    m = sm.Merton(0.02, 0.2, 2.0, -0.1, 0.2, torch.tensor([1.]), dim=1)
+    sol = sm.JumpEulerSolver(m, 1.0, 4)
+    c = mlmc_replay_case(sm, torch, sol, 32, (8, 4), seed=41, full=True)
+    c.update(max_jumps=np.int64(sol.max_jumps), exact_jumps=np.int64(0))
+    np.savez_compressed(os.path.join(HERE, 'mlmc_cols_merton1d.npz'), **{k: np.asarray(v) for k, v in c.items()})
+    ind = make_indep_merton(sm, torch, 0.02, [0.2, 0.3], [1.0, 1.0], -0.05, 0.15, 0.5)
+    sol = sm.JumpEulerSolver(ind, 1.0, 8)
+    c = mlmc_replay_case(sm, torch, sol, 32, (16, 8), seed=42, one_asset=True, full=True)
+    c.update(max_jumps=np.int64(sol.max_jumps), exact_jumps=np.int64(0))
+    np.savez_compressed(os.path.join(HERE, 'mlmc_cols_indep2d.npz'), **{k: np.asarray(v) for k, v in c.items()})
+    g = sm.Gbm(0.02, torch.tensor([0.2, 0.25]), torch.tensor([1., 1.5]), 2, corr_matrix=sm.get_corr_matrix([-0.3]))
+    sol = sm.EulerSolver(g, 1.0, 4)
+    torch.manual_seed(43)
+    (pf, pc), normals = sol.multilevel_solve(32, (8, 4))
+    np.savez_compressed(os.path.join(HERE, 'mlmc_cols_gbm_uniform.npz'), bs=np.int64(32), fine=np.int64(8),
+                        coarse=np.int64(4), normals=normals.numpy().astype(np.float32),
+                        paths_fine=pf.numpy().astype(np.float32), paths_coarse=pc.numpy().astype(np.float32),
+                        h_fine=np.float32(torch.tensor(1.0 / 8).item()),
+                        h_coarse=np.float32((2 * torch.tensor(1.0 / 8)).item()))
+
+
+def optimal_trials_fixture(sm, torch):
+    """get_optimal_trials (sde_mc/mlmc.py:77-97) on prescribed level samples.
+    A stand-in solver returns paths whose terminal values are the samples
+    (the coarse paths are zero), the payoff is EuroCall(0) (the identity on
+    positive values) and the discounter is 1, so the reference's own float32
+    variance and allocation arithmetic runs on known inputs.  Also records
+    that the call leaves solver.num_steps at levels[0]."""
+    rng = np.random.default_rng(21)
+    cases = []
+    for levels, eps, nsamp, scale in [([4, 8, 16, 32, 64, 128, 256], 1e-3 * 0.2, 256, 0.3),
+                                      ([2, 4, 8], 5e-3, 100, 1.0), ([16, 64, 256], 2e-4, 64, 0.05)]:
+        samples = []
+        for lvl in range(len(levels)):
+            # level variances falling with the step size, as for a convergent scheme
+            v = np.abs(rng.standard_normal(nsamp)) * scale * (0.5 ** lvl) + 1e-3
+            samples.append(v.astype(np.float32))
+
+        class FixedSolver:
+            time_interval = 1.0
+            num_steps = 999
+
+            def solve(self, bs, low_storage=False):
+                return torch.from_numpy(samples[0]).reshape(-1, 1, 1), None
+
+            def multilevel_solve(self, bs, pair):
+                i = levels.index(pair[0])
+                fine = torch.from_numpy(samples[i]).reshape(-1, 1, 1)
+                return (fine, torch.zeros_like(fine)), None
+
+        solver = FixedSolver()
+        trials = sm.get_optimal_trials(nsamp, levels, eps, solver, sm.EuroCall(0.0), lambda t: 1.0)
+        cases.append(dict(levels=levels, eps=eps, T=1.0, samples=[a.tolist() for a in samples],
+                          trials=[int(t) for t in trials], num_steps_after=int(solver.num_steps)))
+    with open(os.path.join(HERE, 'optimal_trials.json'), 'w') as fh:
+        json.dump(cases, fh)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--ref', required=True, help='checkout of the sde_mc reference to import')
     ap.add_argument('--skip-stats', action='store_true')
-    ap.add_argument('--only', choices=['cv_jumps', 'heston_asian', 'diffusions', 'levy_mlmc', 'model_stats'],
+    ap.add_argument('--only', choices=['cv_jumps', 'heston_asian', 'diffusions', 'levy_mlmc', 'model_stats',
+                                       'optimal_trials', 'mlmc_columns'],
                     default=None,
                     help='write only these fixtures')
     args = ap.parse_args()
@@ -362,10 +436,18 @@ def main():
     if args.only == 'model_stats':
         model_stats(sm, torch)
         return
+    if args.only == 'optimal_trials':
+        optimal_trials_fixture(sm, torch)
+        return
+    if args.only == 'mlmc_columns':
+        mlmc_columns_fixture(sm, torch)
+        return
     cv_jump_fixture(sm, torch)
     heston_asian_fixtures(sm, torch)
     diffusion_fixtures(sm, torch)
     levy_mlmc_fixture(sm, torch)
+    optimal_trials_fixture(sm, torch)
+    mlmc_columns_fixture(sm, torch)
 
     # ------------------------------------------------------------ KATs ----
     kat = {}

@@ -226,3 +226,50 @@ def test_training_with_jump_integrand():
     st_plain = sm.mc_simple(1 << 16, solver, payoff, disc, bs=1 << 16, payoff_time='adapted')
     assert st_cv.sample_std < st_plain.sample_std * math.sqrt(2)
     assert abs(st_cv.sample_mean - st_plain.sample_mean) < 3 * math.hypot(st_cv.sample_std, st_plain.sample_std)
+
+
+def test_mc_adaptive_cv_trains_coarse_and_prices_fine(oracle_mod):
+    """mc_adaptive_cv (sde_mc/mc.py:245-326): trains the integrand network on a
+    coarse grid, prices fresh paths on the fine grid with the control variate,
+    and returns MCStatistics of the fine run; its mean agrees with the plain
+    estimator on the same grid within 3 standard errors and with the Merton
+    series within 3 standard errors plus the Euler bias."""
+    solver, payoff, disc = merton1d(64, seed=21)
+    f = _net(1, seed=3)
+    opt = torch.optim.Adam(f.parameters(), lr=1e-3)
+    st = sm.mc_adaptive_cv([f, sm.ZeroFunction(1)], opt, solver, (1 << 15, 1 << 17), (16, 64), payoff, disc,
+                           sim_bs=(1 << 15, 1 << 17), bs=(1024, 1024), epochs=3, print_losses=False)
+    assert isinstance(st, sm.MCStatistics)
+    assert st.num_trials == 1 << 17 and solver.num_steps == 64
+    assert st.time_elapsed > 0 and st.sample_std > 0
+    solver.seed = 5
+    plain = sm.mc_simple(1 << 21, solver, payoff, disc, bs=1 << 21, payoff_time='adapted')
+    assert abs(st.sample_mean - plain.sample_mean) < 3 * math.hypot(st.sample_std, plain.sample_std)
+    # the network pays: the control-variate run's standard error beats the
+    # plain estimator's at the same path count
+    assert st.sample_std < plain.sample_std * math.sqrt((1 << 21) / (1 << 17))
+    exact = oracle_mod.merton_call(1.0, 1.0, 1.0, 0.02, 0.2, -0.1, 0.2, 2.0)
+    assert abs(st.sample_mean - exact) < 3 * st.sample_std + 3e-4
+
+
+def test_run_cv_mc_sizes_the_run_for_the_tolerance(oracle_mod):
+    """run_cv_mc (sde_mc/mc.py:443-467) on the MertonEuroCall preset: trains on
+    a grid step_factor times coarser, restores the step count, sizes the run
+    from a control-variate pilot for a 95% half-width eps (a multiple of
+    nn_bs), and returns (MCStatistics, train time, test time)."""
+    problem = sm.MertonEuroCall.default_params(48, 'cuda')
+    f = _net(1, seed=8)
+    opt = torch.optim.Adam(f.parameters(), lr=1e-3)
+    eps = 2e-3
+    st, train_t, test_t = sm.run_cv_mc(problem, [f, sm.ZeroFunction(1)], opt, eps, 1 << 15, step_factor=4,
+                                       sim_bs=1 << 16, train_bs=1024, nn_bs=1024, epochs=3, print_losses=False,
+                                       init_trials=1 << 15)
+    assert isinstance(st, sm.MCStatistics) and train_t > 0 and test_t > 0
+    assert problem.solver.num_steps == 48
+    assert st.num_trials % 1024 == 0
+    assert 1.96 * st.sample_std <= eps * 1.15
+    plain = sm.mc_simple(1 << 22, problem.solver, problem.payoff, problem.discounter, bs=1 << 22,
+                         payoff_time='adapted')
+    assert abs(st.sample_mean - plain.sample_mean) < 3 * math.hypot(st.sample_std, plain.sample_std)
+    exact = oracle_mod.merton_call(1.0, 1.0, 3.0, 0.02, 0.2, -0.05, 0.3, 1.0)
+    assert abs(st.sample_mean - exact) < 3 * st.sample_std + 5e-3

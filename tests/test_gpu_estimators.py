@@ -8,6 +8,7 @@ import pytest
 import torch
 
 import sde_mc_gb300 as sm
+from oracle import oracle
 from tests.cases import gbm_uniform, indep2d, merton1d, merton2d_corr
 
 pytestmark = pytest.mark.gpu
@@ -79,6 +80,14 @@ def test_c2_mlmc(ref_stats):
     trials = sm.get_optimal_trials(1 << 14, levels, 1e-3, solver, payoff, disc)
     assert len(trials) == 5 and all(isinstance(t, int) and t > 0 for t in trials)
     assert trials[0] > trials[-1]
+    # as the reference, the call leaves the solver at the coarsest level (sde_mc/mlmc.py:82)
+    assert solver.num_steps == levels[0]
+    # the allocation of the pilot's own level variances, against the oracle's
+    # FP64 restatement of Giles' formula (the reference rounds in float32)
+    pilot = level_estimates([1 << 14] * 5, levels, solver, payoff, disc)
+    var = [v for _, v in pilot]
+    ora = oracle.optimal_trials(var, levels, solver.time_interval, 1e-3)
+    assert np.all(np.abs(np.asarray(trials) - ora) <= np.maximum(1, 1e-5 * ora)), (trials, ora)
 
 
 def test_solver_layouts_match_reference():

@@ -15,10 +15,11 @@ import numpy as np
 import pytest
 import torch
 
+import sde_mc_gb300 as sm
 from sde_mc_gb300 import _native as N
 from sde_mc_gb300 import kernels as K
 from tests.cases import (FIXTURE_CASES, asian_merton, basket, double_gbm, gbm_uniform, heston, indep2d, inst_for,
-                         levy2d, merton1d, merton2d_corr, zdim)
+                         levy2d, levy2d_exact, merton1d, merton2d_corr, zdim)
 from tests.conftest import load_npz
 from tests.test_oracle import expected_jump_paths
 
@@ -85,6 +86,91 @@ def test_mlmc_replay_matches_reference(name, factory, levels):
     np.testing.assert_array_equal(np_(out["xc"]), fx["xc"])
 
 
+@pytest.mark.parametrize("name,factory,levels,exact", [
+    ("mlmc_asian_merton", lambda: asian_merton(4), (8, 4), True),
+    ("mlmc_levy2d_exact", lambda: levy2d_exact(4), (8, 4), False)])
+def test_mlmc_replay_asian_and_levy_exact_jumps(name, factory, levels, exact, oracle_mod):
+    """K2 on the last two couplings recorded from the reference: the Asian
+    wrapper around Merton (sde_mc/sde.py:378-406) and the LevyRainbowMLMC
+    preset (Levy 'indep', exact_jumps=True, factor 2; sde_mc/problem.py:93-106,
+    coupling loop sde_mc/solvers.py:228-307).  GPU == oracle bit for bit; the
+    Asian coupling also == the reference's recorded states bit for bit, the
+    Levy one within 1e-5 (its drift folds -f*gamma into one coefficient)."""
+    fx = load_npz(name)
+    inst = inst_for(factory(), num_paths=int(fx["bs"]), steps=levels[1])
+    asset = torch.from_numpy(fx["asset"]) if "asset" in fx else None
+    out = K.mlmc_replay(inst, levels[0], levels[1], float(fx["h_fine"]), float(fx["h_coarse"]),
+                        torch.from_numpy(fx["dw"]), fx["marks"].shape[1], torch.from_numpy(fx["jump_times"]),
+                        torch.from_numpy(fx["marks"]), asset)
+    assert int(out["status"].item()) == 0
+    ref = oracle_mod.mlmc_replay(inst, levels[0] // levels[1], float(fx["h_fine"]), float(fx["h_coarse"]),
+                                 fx["dw"], fx["marks"].shape[1], fx["jump_times"], fx["marks"], fx.get("asset"))
+    for k in ("xf", "xc"):
+        np.testing.assert_array_equal(np_(out[k]), ref[k])
+        if exact:
+            np.testing.assert_array_equal(np_(out[k]), fx[k])
+        else:
+            np.testing.assert_allclose(np_(out[k]), fx[k], rtol=1e-5, atol=1e-6)
+
+
+@pytest.mark.parametrize("name,factory,levels", [("mlmc_cols_merton1d", lambda: merton1d(4), (8, 4)),
+                                                 ("mlmc_cols_indep2d", lambda: indep2d(8), (16, 8)),
+                                                 ("mlmc_cols_gbm_uniform", lambda: gbm_uniform(4), (8, 4))])
+def test_mlmc_columns_match_reference(name, factory, levels):
+    """Every column multilevel_solve returns, replayed from the reference's own
+    draws: the jump-adapted grid's fine and coarse states after each coarse
+    step up to the batch's last (sde_mc/solvers.py:228-307), and the uniform
+    grid's every fine and coarse state (:90-119) — bit for bit."""
+    fx = load_npz(name)
+    inst = inst_for(factory(), num_paths=int(fx["bs"]), steps=levels[1])
+    hf, hc = float(fx["h_fine"]), float(fx["h_coarse"])
+    if inst.grid == N.GRID_UNIFORM:
+        cols = (levels[0] + 1, levels[1] + 1)
+        out = K.mlmc_replay(inst, levels[0], levels[1], hf, hc, torch.from_numpy(fx["normals"]), levels[1], cols=cols)
+        total = None
+    else:
+        c = levels[1] + int(fx["max_jumps"]) + 1
+        asset = torch.from_numpy(fx["asset"]) if "asset" in fx else None
+        out = K.mlmc_replay(inst, levels[0], levels[1], hf, hc, torch.from_numpy(fx["dw"]), fx["marks"].shape[1],
+                            torch.from_numpy(fx["jump_times"]), torch.from_numpy(fx["marks"]), asset, cols=(c, c))
+        total = int(np_(out["steps"]).max())
+        assert total + 1 == fx["paths_fine"].shape[1]
+    assert int(out["status"].item()) == 0
+    pf, pc = np_(out["paths_fine"]), np_(out["paths_coarse"])
+    if total is not None:
+        pf, pc = pf[:, :total + 1], pc[:, :total + 1]
+    np.testing.assert_array_equal(pf, fx["paths_fine"])
+    np.testing.assert_array_equal(pc, fx["paths_coarse"])
+
+
+@pytest.mark.parametrize("factory,levels", [(lambda: indep2d(8), (16, 8)), (lambda: merton2d_corr(6), (12, 6)),
+                                            (lambda: gbm_uniform(6), (24, 6)), (lambda: heston(4), (16, 4))])
+def test_multilevel_solve_returns_every_column(factory, levels):
+    """multilevel_solve's drop-in shapes and contents on the kernels' own
+    draws: the first column is the initial state, the last the terminal states
+    the estimators' level kernels compute (bit for bit); on the jump-adapted
+    grid the batch has total_steps_coarse + 1 columns with finished paths
+    frozen; on the uniform grid fine + 1 and coarse + 1 columns and the fine
+    increments, whose sums drive the coarse steps."""
+    solver = factory()[0]
+    bs = 300
+    (pf, pc), nz = solver.multilevel_solve(bs, levels)
+    d = solver.sde.dim
+    x0 = torch.as_tensor(solver.sde.init_value, dtype=torch.float32).reshape(1, d).expand(bs, d)
+    np.testing.assert_array_equal(np_(pf[:, 0]), np_(x0))
+    np.testing.assert_array_equal(np_(pc[:, 0]), np_(x0))
+    (tf, tc), _ = solver.multilevel_terminals(bs, levels)
+    np.testing.assert_array_equal(np_(pf[:, -1]), np_(tf[:, -1]))
+    np.testing.assert_array_equal(np_(pc[:, -1]), np_(tc[:, -1]))
+    if solver.has_jumps:
+        assert nz is None and pf.shape == pc.shape and pf.shape[0] == bs and pf.shape[2] == d
+        assert pf.shape[1] >= levels[1] + 1
+    else:
+        assert pf.shape == (bs, levels[0] + 1, d) and pc.shape == (bs, levels[1] + 1, d)
+        assert tuple(nz.shape[:3]) == (bs, levels[0], d)
+        assert torch.isfinite(nz).all() and np_(nz).std() > 0
+
+
 @pytest.mark.parametrize("name,levels", [("mlmc_heston", (8, 4)), ("mlmc_heston_f4", (16, 4))])
 def test_mlmc_replay_heston(name, levels, oracle_mod):
     """K2's uniform-grid coupled Heston levels equal the oracle's bit for bit
@@ -122,7 +208,20 @@ EXPORT_CASES = {
     "double_gbm": lambda: double_gbm(3, 10),
     "heston": lambda: heston(24),
     "asian_merton": lambda: asian_merton(20),
+    # the remaining payoff branches of the kernels' payoff() (sde_mc/options.py:179-321)
+    "put1d": lambda: _with_payoff(merton1d(60), sm.EuroPut(1.05)),
+    "binary_aon1d": lambda: _with_payoff(merton1d(60), sm.BinaryAoN(1.0)),
+    "digital1d": lambda: _with_payoff(merton1d(60), sm.Digital(0.95)),
+    "bestof3": lambda: _with_payoff(basket(3, 32), sm.BestOf(1.1)),
+    "basket4_geometric": lambda: _with_payoff(basket(4, 24), sm.Basket(1.0, average_type="geometric")),
+    "heston_rainbow": lambda: _with_payoff(heston(24), sm.HestonRainbow(1.0)),
 }
+# payoffs through CUDA's logf/expf, which may round the last bit apart from libm's
+LIBM_PAYOFFS = {"basket4_geometric"}
+
+
+def _with_payoff(case, payoff):
+    return case[0], payoff, case[2]
 
 
 def _export(name, n=1000, seed=77):
@@ -146,8 +245,13 @@ def test_materialise_matches_oracle_step_by_step(name, oracle_mod):
     ref = oracle_mod.from_export(inst, g["z"], S, g.get("jt"), g.get("jm"), g.get("jsel"), exact=False)
     assert ref["rc"] == 0
     np.testing.assert_array_equal(g["steps"], ref["steps"])
-    for key in ("paths", "left", "time", "jumps", "normals", "payoffs"):
+    for key in ("paths", "left", "time", "jumps", "normals"):
         np.testing.assert_array_equal(g[key], ref[key], err_msg=key)
+    if name in LIBM_PAYOFFS:
+        np.testing.assert_allclose(g["payoffs"], ref["payoffs"], rtol=1e-6, atol=1e-6)
+    else:
+        np.testing.assert_array_equal(g["payoffs"], ref["payoffs"])
+    assert np.count_nonzero(g["payoffs"]) > 0
 
 
 @pytest.mark.parametrize("name", list(EXPORT_CASES))
