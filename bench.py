@@ -62,7 +62,6 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--plain-windows", type=int, default=10,
                     help="windows of the stream the plain one-request-per-launch server replays")
     ap.add_argument("--sections", default="rainbow,materialise,mlmc,mix,cv,accuracy",
@@ -226,80 +225,134 @@ def stream_windows(first, count):
     return S.make_stream(RATE, (first + count) * WINDOW_S, seed=1, t_begin=first * WINDOW_S)
 
 
-def oracle_serve(stream, budget_s, threads=None):
-    """The plain method on the host cores through the oracle port (the CPU
-    restatement of the reference's algorithm, all threads), request by request
-    in arrival order until budget_s is spent.  A main run longer than its
-    share of the budget is timed on a prefix of its paths and extrapolated
-    linearly (CPU time is proportional to paths).  Returns (seconds per
-    request, requests timed, threads, paths timed)."""
+CPU_SAMPLE = 32          # requests of the stream both arms time on the host cores
+CPU_SHARE_S = 0.5        # host seconds a main run is simulated for before extrapolating
+CPU_PREFIX = 4096        # pilot paths simulated before extrapolating
+
+
+def cpu_sample():
+    """The fixed CPU sample both bench arms time: the stream's first
+    CPU_SAMPLE requests (window 0)."""
+    return stream_windows(0, 1)[:CPU_SAMPLE]
+
+
+def cpu_price_request(r, threads):
+    """Host seconds of one request priced by the plain method (run_mc: pilot
+    sizes the main run, sde_mc/mc.py:418-440) through the oracle port on
+    `threads` host threads.  The pilot is simulated on its first CPU_PREFIX
+    paths and the main run on at most max(4096, CPU_SHARE_S / per-path time)
+    paths; both times are extrapolated linearly to the full path counts (CPU
+    time is proportional to paths).  Deterministic work: the same paths, the
+    same sizes, on every run.  Returns (seconds, paths simulated)."""
     from oracle import oracle
-    threads = threads or os.cpu_count() or 1
-    spent, times, paths = 0.0, [], 0
-    for r in stream:
-        if spent >= budget_s and times:
-            break
-        n0 = int(r.inst.num_paths)
+    n0 = int(r.inst.num_paths)
+    k0 = min(n0, CPU_PREFIX)
+    t = time.perf_counter()
+    out, _, _ = oracle.price(r.phase(k0, 0), nthreads=threads)
+    t_prefix = time.perf_counter() - t
+    per_path = t_prefix / max(k0, 1)
+    mean0, var0 = float(out[3]), float(out[4])
+    eps = r.target * abs(mean0)
+    n = max(64, math.ceil(1.96 ** 2 * var0 / eps ** 2)) if var0 > 0 and eps > 0 else 0
+    m = min(n, max(4096, int(CPU_SHARE_S / max(per_path, 1e-12))))
+    t_main = 0.0
+    if m > 0:
         t = time.perf_counter()
-        out, _, _ = oracle.price(r.phase(n0, 0), nthreads=threads)
-        t_pilot = time.perf_counter() - t
-        mean0, var0 = float(out[3]), float(out[4])
-        eps = r.target * abs(mean0)
-        n = max(64, math.ceil(1.96 ** 2 * var0 / eps ** 2)) if var0 > 0 and eps > 0 else 0
-        per_path = t_pilot / max(n0, 1)
-        share = max(budget_s / 6.0, 0.5)
-        m = min(n, n if n * per_path <= share else max(4096, int(share / max(per_path, 1e-12))))
-        t_main = 0.0
-        if m > 0:
-            t = time.perf_counter()
-            oracle.price(r.phase(m, n0), nthreads=threads)
-            dt = time.perf_counter() - t
-            t_main = dt * (n / m)
-            spent += dt
-        spent += t_pilot
-        paths += n0 + m
-        times.append(t_pilot + t_main)
-    return statistics.mean(times), len(times), threads, paths
+        oracle.price(r.phase(m, n0), nthreads=threads)
+        t_main = (time.perf_counter() - t) * (n / m)
+    return per_path * n0 + t_main, k0 + m
+
+
+def cpu_baseline_of(reqs, threads):
+    """(seconds per request, paths simulated) over a list of requests."""
+    secs, paths = [], 0
+    for r in reqs:
+        s_, p_ = cpu_price_request(r, threads)
+        secs.append(s_)
+        paths += p_
+    return statistics.mean(secs), paths
+
+
+CPU_KIND = ("oracle port: the C restatement of the reference's algorithm (its jump-adapted Euler loop, "
+            "payoff and estimator), plain estimator, on the host cores; pilot and main runs timed on a prefix "
+            "of their paths and extrapolated")
+REFERENCE_TORCH_NOTE = ("the reference's own torch CPU path is not installed on this box; in the build container "
+                        "(8 x86 threads) it priced config 1 (1-D Merton, 2^16 paths, 100 steps) in 0.64 s")
 
 
 def run_reference(args):
-    """`--impl reference`: the stream's requests priced by the plain method on
-    the host cores (oracle port); one step = one bounded sample of requests."""
+    """`--impl reference`: the plain method on the host cores (oracle port)
+    over the same fixed sample of the stream's requests as the main arm's
+    cpu_baseline, each request timed once: the timed steps partition the
+    sample; warm-up steps price the first requests' pilots untimed."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    from sde_mc_gb300 import stream as S
-    reqs = S.make_stream(RATE, 0.05, seed=1)
-    per_step = max(args.cpu_seconds / max(args.steps + args.warmup, 1), 1.0)
-    secs, walls, n_req, threads = [], [], 0, os.cpu_count() or 1
-    pos = 0
-    for i in range(args.warmup + args.steps):
-        chunk = reqs[pos:] + reqs[:pos]
+    from oracle import oracle
+    reqs = cpu_sample()
+    threads = os.cpu_count() or 1
+    for r in reqs[:max(args.warmup, 0)]:
+        oracle.price(r.phase(min(int(r.inst.num_paths), CPU_PREFIX), 0), nthreads=threads)
+    steps = max(args.steps, 1)
+    groups = [reqs[i * len(reqs) // steps:(i + 1) * len(reqs) // steps] for i in range(steps)]
+    secs, walls, paths = [], [], 0
+    for g in groups:
         t0 = time.perf_counter()
-        spr, n, threads, _ = oracle_serve(chunk, per_step)
-        wall = time.perf_counter() - t0
-        pos = (pos + n) % len(reqs)
-        if i >= args.warmup:
-            secs.append(spr)
-            walls.append(wall)
-            n_req += n
+        for r in g:
+            s_, p_ = cpu_price_request(r, threads)
+            secs.append(s_)
+            paths += p_
+        walls.append(time.perf_counter() - t0)
     sec_per_price = statistics.mean(secs)
     value = 1.0 / sec_per_price
+    # config 1 on the same port and threads, for reading the port against the reference's torch timing
+    import torch
+    import sde_mc_gb300 as sm
+    from sde_mc_gb300.lowering import lower
+    m = sm.Merton(0.02, 0.2, 2.0, -0.1, 0.2, torch.tensor([1.]), dim=1)
+    c1 = lower(sm.JumpEulerSolver(m, 1.0, 100), sm.EuroCall(1.0), sm.ConstantShortRate(0.02), num_paths=1 << 16)
+    t0 = time.perf_counter()
+    oracle.price(c1, nthreads=threads)
+    c1_s = time.perf_counter() - t0
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(walls) * 1e3,
             "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": {"workload": WORKLOAD, "form": "plain run_mc per request",
-                                            "step": "one bounded sample of the stream's requests (%.1f s of host "
-                                                    "work); value = requests / their pilot + main time, long "
-                                                    "main runs timed on a prefix of their paths and "
-                                                    "extrapolated" % per_step,
-                                            "ms_per_price": sec_per_price * 1e3},
+            "data": "synthetic", "reference_kind": CPU_KIND,
+            "config": {"workload": WORKLOAD, "form": "plain run_mc per request (oracle port, host cores)",
+                       "step": "a share of the fixed %d-request sample (the stream's first requests), each "
+                               "request timed once; value = requests / their pilot + main time" % len(reqs),
+                       "ms_per_price": sec_per_price * 1e3, "config1_port_s": c1_s, "threads": threads},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": "%d stream requests (pilot + main, plain estimator) on %d threads; main "
-                                       "runs over their share of %.1f s per step timed on a prefix of paths and "
-                                       "extrapolated" % (n_req, threads, per_step)},
+                             "sample": "the stream's first %d requests (pilot + main, plain estimator, %d paths "
+                                       "simulated, extrapolated to the full counts) on %d threads"
+                                       % (len(reqs), paths, threads),
+                             "config1_port_s": c1_s, "reference_torch": REFERENCE_TORCH_NOTE},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+def csrc_digest():
+    """Digest of the kernel sources (csrc and the ABI header): an ncu figure in
+    profiles/ is reported only when it was captured from these sources."""
+    import hashlib
+    h = hashlib.sha256()
+    base = os.path.join(ROOT, "sde_mc_gb300", "csrc")
+    for f in sorted(os.listdir(base)):
+        if f.endswith((".cu", ".cuh")):
+            with open(os.path.join(base, f), "rb") as fh:
+                h.update(f.encode() + b"\0" + fh.read())
+    with open(os.path.join(ROOT, "include", "sdemc.h"), "rb") as fh:
+        h.update(fh.read())
+    return h.hexdigest()[:16]
+
+
+def profiled(kernel):
+    """The ncu record of `kernel` in profiles/kernel_traffic.json when it was
+    captured from the current kernel sources, else None."""
+    rec = (load_json_file(os.path.join("profiles", "kernel_traffic.json")) or {}).get(kernel)
+    if rec and rec.get("csrc_digest") == csrc_digest():
+        return rec
+    return None
 
 
 # ------------------------------------------------------------ sections ----
@@ -366,7 +419,7 @@ def bench_rainbow_plain(dev, steps, warmup, fp32_peak, mufu_peak):
     achieved = flops / kernel_s / 1e12
     mufu_ops = n_target * steps_per_path * mufu_per_path_step(2, 2.0 / steps_per_path)
     mufu_achieved = mufu_ops / kernel_s / 1e12
-    traffic = (load_json_file(os.path.join("profiles", "kernel_traffic.json")) or {}).get("price_kernel<2,diag>")
+    traffic = profiled("price_kernel<2,diag>")
     return {"workload": RAINBOW_WORKLOAD, "paths_per_price": n_target, "steps_per_path": steps_per_path,
             "prices_per_s": steps / (sum(k_ms) + sum(r_ms)) * 1e3, "ms_per_price": statistics.mean(
                 [a + b for a, b in zip(k_ms, r_ms)]),
@@ -376,8 +429,9 @@ def bench_rainbow_plain(dev, steps, warmup, fp32_peak, mufu_peak):
             "roofline": bind_roofline({"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                          "frac": achieved / fp32_peak,
                          "traffic": traffic["dram_bytes"] if traffic else None,
-                         "traffic_note": "DRAM bytes of one ncu-captured launch (2^20 paths): descriptor and "
-                                         "chunk partials only; paths stay in registers",
+                         "traffic_note": "DRAM bytes of one ncu-captured launch (2^20 paths) of these kernel "
+                                         "sources (null when profiles/ holds no capture of them): descriptor "
+                                         "and chunk partials only; paths stay in registers",
                          "issue_active_ncu": traffic.get("issue_active") if traffic else None,
                          "issue_note": "share of cycles an instruction issued (ncu, profiles/): the path loop is "
                                        "issue-bound, mostly Philox's integer rounds, which count as no flop",
@@ -743,14 +797,28 @@ def bench_served(dev, steps, warmup, plain_windows, rank=0, world=1):
 
 
 def profile_serve(seconds):
+    """The served stream for `seconds` seconds (600 windows = the full 60 s
+    stream of the served-stream workload): prices/s, p50/p99 per 10 s segment
+    (does the server drift?), the tick-duration histogram and the server's
+    counters."""
+    import numpy as np
     import torch
     from sde_mc_gb300 import serve
     from sde_mc_gb300 import stream as S
     reqs = S.make_stream(RATE, seconds, seed=1)
-    with serve.Server(max_slots=4096, mem_budget=40 << 30, side_streams=4) as srv:
-        _, summ = S.run_served(reqs, srv)
-        summ["stats"] = srv.stats()
+    with serve.Server(max_slots=4096, mem_budget=40 << 30, side_streams=4, policy="srpt") as srv:
+        res, summ = S.run_served(reqs, srv)
+        st = srv.stats()
     torch.cuda.synchronize()
+    segs = []
+    for a in range(0, int(math.ceil(seconds)), 10):
+        lat = [res[r.idx].latency_s for r in reqs if a <= r.t < a + 10]
+        if lat:
+            segs.append({"from_s": a, "requests": len(lat), "p50_ms": float(np.percentile(lat, 50) * 1e3),
+                         "p99_ms": float(np.percentile(lat, 99) * 1e3)})
+    edges = ["<0.125"] + ["%g-%g" % (0.125 * 2 ** (b - 1), 0.125 * 2 ** b) for b in range(1, 15)] + [">=2048"]
+    summ.update(stats=st, segments=segs, busy_prices_per_s=len(reqs) / st["busy_s"],
+                tick_ms_hist={e: n for e, n in zip(edges, st["tick_hist"]) if n})
     print(json.dumps(summ))
 
 
@@ -864,7 +932,17 @@ def main():
                    "requests": n_req, "windows": args.steps, "window_s": WINDOW_S, "arrival_rate": RATE,
                    "l2": "inputs are descriptors; L2 flushed (256 MB write) before the timed stream",
                    "parallelism": ("stream sharded by request index over %d GPUs" % world) if world > 1
-                   else "single GPU"},
+                   else "single GPU",
+                   "vs_plain": {"served_prices_per_s_e2e": e2e, "served_p50_ms": summ["p50_ms"],
+                                "served_p99_ms": summ["p99_ms"], "plain_prices_per_s": plain["prices_per_s"],
+                                "plain_p50_ms": plain["p50_ms"], "plain_p99_ms": plain["p99_ms"],
+                                "speedup_e2e": e2e / plain["prices_per_s"],
+                                "speedup_p50": plain["p50_ms"] / summ["p50_ms"],
+                                "speedup_p99": plain["p99_ms"] / summ["p99_ms"],
+                                "capacity_prices_per_s": b["capacity"]["prices_per_s_e2e"],
+                                "capacity_p99_ms": b["capacity"]["p99_ms"],
+                                "median_vrf": summ.get("vrf_median"),
+                                "cv_share": summ["control_variate_used"] / max(summ["requests"], 1)}},
         "latency_ms": {"p50": summ["p50_ms"], "p99": summ["p99_ms"], "mean": summ["mean_ms"], "max": summ["max_ms"]},
         "served": summ,
         "plain": {"prices_per_s": plain["prices_per_s"], "p50_ms": plain["p50_ms"], "p99_ms": plain["p99_ms"],
@@ -875,12 +953,11 @@ def main():
                              "p50": plain["p50_ms"] / summ["p50_ms"], "p99": plain["p99_ms"] / summ["p99_ms"]},
         "roofline": bind_roofline({"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak,
-                     "traffic": ((load_json_file(os.path.join("profiles", "kernel_traffic.json")) or {})
-                                 .get("serve_kernel<6,0,0,1>") or {}).get("dram_bytes"),
-                     "traffic_note": "DRAM bytes of one ncu-captured serve_kernel launch (d = 6 main run): slot "
+                     "traffic": (profiled("serve_kernel<6,0,0,1>") or {}).get("dram_bytes"),
+                     "traffic_note": "DRAM bytes of one ncu-captured serve_kernel launch (d = 6 main run) of "
+                                     "these kernel sources (null when profiles/ holds no capture of them): slot "
                                      "state and chunk partials only; paths stay in registers",
-                     "issue_active_ncu": ((load_json_file(os.path.join("profiles", "kernel_traffic.json")) or {})
-                                          .get("serve_kernel<6,0,0,1>") or {}).get("issue_active"),
+                     "issue_active_ncu": (profiled("serve_kernel<6,0,0,1>") or {}).get("issue_active"),
                      "issue_note": "share of cycles an instruction issued (ncu, profiles/)",
                      "kernel": "serve_kernel (all classes) over the server's device busy time",
                      "flops": "sum over requests of (pilot + main paths) x (steps + jump rate x T) x F(d)",
@@ -915,11 +992,16 @@ def main():
             line["cv_learned"] = _section(bench_cv_learned, dev)
         if "accuracy" in secs:
             line["accuracy"] = _section(bench_accuracy, dev, line, b)
-        spr, n, threads, paths = oracle_serve(b["timed"], args.cpu_seconds)
+        threads = os.cpu_count() or 1
+        reqs = cpu_sample()
+        spr, paths = cpu_baseline_of(reqs, threads)
         line["cpu_baseline"] = {"value": 1.0 / spr, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": "%d requests of the timed stream (pilot + main, plain estimator, %d paths "
-                                          "simulated) on %d threads; long main runs timed on a prefix of their "
-                                          "paths and extrapolated" % (n, paths, threads)}
+                                "sample": "the stream's first %d requests (pilot + main, plain estimator, %d paths "
+                                          "simulated, extrapolated to the full counts) on %d threads; the "
+                                          "reference arm times the same requests" % (len(reqs), paths, threads),
+                                "method": CPU_KIND, "reference_torch": REFERENCE_TORCH_NOTE}
+        # the comparison the target is stated in, compact and last (read from the end of the output)
+        line["vs_plain"] = dict(line["config"]["vs_plain"])
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()

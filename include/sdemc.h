@@ -538,6 +538,9 @@ typedef struct {
   int64_t launches;         /* kernels launched (install, class, reduce)        */
   int64_t h2d_bytes, d2h_bytes;  /* plan/slot uploads and phase-record readbacks */
   double busy_s;            /* sum of tick durations on the device              */
+  /* tick durations on the device: bucket 0 below 0.125 ms, bucket b in
+     [0.125 * 2^(b-1), 0.125 * 2^b) ms, bucket 15 from 2048 ms up            */
+  int64_t tick_hist[16];
 } sdemc_server_stats;
 
 /* Integrand-weight parameters of SDEMC_EST_LINEAR_CV for one descriptor, as

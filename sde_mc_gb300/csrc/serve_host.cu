@@ -539,6 +539,9 @@ int Server::process(TickBuf& B) {
     std::lock_guard<std::mutex> lk(mu);
     st.ticks++;
     st.busy_s += ms * 1e-3;
+    int b = 0;
+    for (double edge = 0.125; b < 15 && ms >= edge; edge *= 2.0) ++b;
+    st.tick_hist[b]++;
     st.path_steps += (int64_t)B.path_steps;
     st.launches += B.launches;
     st.h2d_bytes += (int64_t)B.n_installs * (int64_t)sizeof(ServeInstall) +

@@ -64,7 +64,7 @@ class ServerStats(ctypes.Structure):
                 ("pending", ctypes.c_int64), ("active", ctypes.c_int64), ("ticks", ctypes.c_int64),
                 ("mem_in_use", ctypes.c_int64), ("mem_peak", ctypes.c_int64), ("path_steps", ctypes.c_int64),
                 ("launches", ctypes.c_int64), ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64),
-                ("busy_s", ctypes.c_double)]
+                ("busy_s", ctypes.c_double), ("tick_hist", ctypes.c_int64 * 16)]
 
 
 def struct_sizes():
@@ -180,7 +180,9 @@ class Server:
     def stats(self):
         s = ServerStats()
         N.check(N.load().sdemc_server_stats_get(self._h, ctypes.byref(s)), "sdemc_server_stats_get")
-        return {f: getattr(s, f) for f, _ in ServerStats._fields_}
+        out = {f: getattr(s, f) for f, _ in ServerStats._fields_}
+        out["tick_hist"] = list(out["tick_hist"])
+        return out
 
     def close(self):
         if getattr(self, "_h", None) is not None:

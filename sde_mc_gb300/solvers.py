@@ -47,6 +47,11 @@ class SdeSolver(ABC):
     def solve(self, bs=1, return_normals=False):
         pass
 
+    def multilevel_terminals(self, bs, levels):
+        """((paths_fine, paths_coarse), None) with only the initial and terminal
+        columns of multilevel_solve's coupled paths (no column storage)."""
+        return _multilevel_terminals(self, bs, levels)
+
     @abstractmethod
     def init_storage(self, bs, steps):
         pass
@@ -182,10 +187,6 @@ class JumpDiffusionSolver(SdeSolver):
         total = int(out["steps"].max().item()) if bs > 0 else 0
         return (self._out(out["paths_fine"][:, :total + 1]), self._out(out["paths_coarse"][:, :total + 1])), None
 
-    def multilevel_terminals(self, bs, levels):
-        """((paths_fine, paths_coarse), None) with only the initial and terminal
-        columns of multilevel_solve (no column storage)."""
-        return _multilevel_terminals(self, bs, levels)
 
 
 def level_steps(solver, fine, coarse):

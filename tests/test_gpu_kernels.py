@@ -154,7 +154,9 @@ def test_multilevel_solve_returns_every_column(factory, levels):
     increments, whose sums drive the coarse steps."""
     solver = factory()[0]
     bs = 300
+    cursor = solver.path_cursor
     (pf, pc), nz = solver.multilevel_solve(bs, levels)
+    solver.path_cursor = cursor  # the same paths again
     d = solver.sde.dim
     x0 = torch.as_tensor(solver.sde.init_value, dtype=torch.float32).reshape(1, d).expand(bs, d)
     np.testing.assert_array_equal(np_(pf[:, 0]), np_(x0))
