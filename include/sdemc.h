@@ -34,7 +34,12 @@ enum {
   SDEMC_EINVAL = 1,        /* bad argument (shape, size, null pointer)          */
   SDEMC_EUNSUPPORTED = 2,  /* model/payoff/dim combination not implemented      */
   SDEMC_ENOMEM = 3,        /* caller buffer too small / admission over budget   */
-  SDEMC_ETIMEOUT = 4,      /* a bounded device loop gave up                     */
+  SDEMC_ETIMEOUT = 4,      /* a bounded device wait gave up (tensor-core
+                              kernels): the kernel stopped and freed its tensor
+                              memory while its last product may still have been
+                              writing it, so every output of that launch, and of
+                              any other tensor-core launch that ran on the device
+                              at the same time, is void and must be discarded  */
   SDEMC_ECUDA = 5,         /* CUDA runtime error                                */
   SDEMC_EOVERFLOW = 6      /* a path needed more steps/jumps than storage holds */
 };

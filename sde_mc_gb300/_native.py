@@ -180,6 +180,10 @@ def status_error(st, what):
     st = int(st)
     if st == OK:
         return
+    if st == ETIMEOUT:
+        raise TimeoutError("%s: a bounded tensor-core wait gave up; every output of that launch, and of any "
+                           "tensor-core launch that ran on the device at the same time, is void and must be "
+                           "discarded" % what)
     if st & EOVERFLOW == EOVERFLOW:
         raise IndexError("%s: a path needed more steps/jumps than its storage or iteration cap "
                          "(the reference raises IndexError when its pre-drawn jump times run out)" % what)

@@ -256,14 +256,18 @@ extern "C" int sdemc_price_batch(const void* h_blob, const void* d_blob, void* d
   int rc = check_cuda(cudaMemsetAsync(sc, 0, S.part, s), "clear batch counters");
   if (rc) return rc;
   EventPool* ev = nullptr;
+  int forked = 0;  // side streams that wait on the fork event and must be joined back
   if (n_side > 0) {
     if ((rc = events_for_device(&ev))) return rc;
     if ((rc = check_cuda(cudaEventRecord(ev->fork, s), "fork record"))) return rc;
-    for (int j = 0; j < n_side; ++j)
-      if ((rc = check_cuda(cudaStreamWaitEvent((cudaStream_t)side_streams[j], ev->fork, 0), "fork wait")))
-        return rc;
+    for (int j = 0; j < n_side && rc == SDEMC_OK; ++j) {
+      rc = check_cuda(cudaStreamWaitEvent((cudaStream_t)side_streams[j], ev->fork, 0), "fork wait");
+      if (rc == SDEMC_OK) ++forked;
+    }
   }
-  for (int k = 0; k < H.n_class; ++k) {
+  // a failure after the fork still joins every forked side stream back into
+  // `stream` (under stream capture an unjoined fork invalidates the graph)
+  for (int k = 0; k < H.n_class && rc == SDEMC_OK; ++k) {
     const sdemc_batch_class& C = cls[k];
     BatchParams B;
     B.insts = reinterpret_cast<const sdemc_inst*>(db + H.off_insts);
@@ -278,14 +282,18 @@ extern "C" int sdemc_price_batch(const void* h_blob, const void* d_blob, void* d
     const int64_t chunks = C.chunk_end - C.chunk_begin;
     if (chunks == 0) continue;
     cudaStream_t ks = n_side > 0 ? (cudaStream_t)side_streams[k % n_side] : s;
-    if ((rc = launch_class(C.dim, C.noise, C.mode, B, h_cfgs ? &h_cfgs[k] : nullptr, chunks, ks))) return rc;
+    rc = launch_class(C.dim, C.noise, C.mode, B, h_cfgs ? &h_cfgs[k] : nullptr, chunks, ks);
   }
-  if (n_side > 0) {
-    for (int j = 0; j < n_side; ++j) {
-      if ((rc = check_cuda(cudaEventRecord(ev->join[j], (cudaStream_t)side_streams[j]), "join record"))) return rc;
-      if ((rc = check_cuda(cudaStreamWaitEvent(s, ev->join[j], 0), "join wait"))) return rc;
+  if (forked > 0) {
+    const int err = rc;
+    for (int j = 0; j < forked; ++j) {
+      int jr = check_cuda(cudaEventRecord(ev->join[j], (cudaStream_t)side_streams[j]), "join record");
+      if (jr == SDEMC_OK) jr = check_cuda(cudaStreamWaitEvent(s, ev->join[j], 0), "join wait");
+      if (rc == SDEMC_OK) rc = jr;
     }
+    if (err != SDEMC_OK) return err;
   }
+  if (rc != SDEMC_OK) return rc;
   BatchReduceParams R;
   R.chunk_prefix = reinterpret_cast<const int64_t*>(db + H.off_chunk_prefix);
   R.group_prefix = reinterpret_cast<const int64_t*>(db + H.off_group_prefix);
