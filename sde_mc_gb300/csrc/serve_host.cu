@@ -15,8 +15,14 @@
 //      finished phases: a pilot sizes the main run (find_num_trials,
 //      sde_mc/mc.py:418-427) and fits the control-variate coefficients; a
 //      main run becomes a result.
-// Two tick buffers alternate, so the next tick is queued before the running
-// one ends and the device does not wait for the host.
+// Two tick buffers alternate, each with its own stream and side streams, so
+// the next tick is queued before the running one ends and its class kernels
+// start while the running tick's last kernels drain: a class kernel reads only
+// its entries and the slots' descriptors and coefficients (no running tick
+// writes those), and the one ordering across ticks — each slot's FP64 sums are
+// folded tick after tick — is kept by making each tick's reduction wait for
+// the previous tick's.  The device busy time is the union of the ticks'
+// intervals on one device timeline.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -121,6 +127,11 @@ struct HostSlot {
 };
 
 struct TickBuf {
+  cudaStream_t stream = nullptr;          // the tick's own stream
+  std::vector<cudaStream_t> side;         // class kernels spread over these
+  cudaEvent_t fork = nullptr, red_done = nullptr;
+  std::vector<cudaEvent_t> join;
+  int64_t seq = -1;                       // tick number (index into the end-stamp ring)
   ServeEntry* entries_h = nullptr;
   ServeInstall* installs_h = nullptr;
   ServeDone* done_h = nullptr;
@@ -129,7 +140,7 @@ struct TickBuf {
   ServeDone* done_d = nullptr;
   unsigned long long* counters_d = nullptr;
   double* part_d = nullptr;
-  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  cudaEvent_t t0 = nullptr;  // tick start (the end is its stamp in the ring)
   int n_entries = 0, n_installs = 0, n_done = 0, launches = 0;
   double path_steps = 0.0;
 };
@@ -211,12 +222,14 @@ struct Server {
   int threads = 128;
   int64_t part_cap = 0;  // doubles per tick buffer
   int64_t fixed_bytes = 0;
-  cudaStream_t stream = nullptr;
-  std::vector<cudaStream_t> side;
-  cudaEvent_t fork = nullptr;
-  std::vector<cudaEvent_t> join;
   ServeSlot* slots_d = nullptr;
   TickBuf buf[2];
+  // tick-end stamps: a ring longer than the two ticks in flight, so the
+  // previous tick's end is still recorded when a tick is processed
+  static constexpr int kStamps = 4;
+  cudaEvent_t stamp[kStamps] = {};
+  int64_t ticks_enqueued = 0;
+  double end_prev_ms = 0.0, last_end_ms = 0.0;  // device timeline of processed ticks
 
   std::vector<HostSlot> hs;
   std::vector<int> free_slots;
@@ -237,7 +250,7 @@ struct Server {
   void loop();
   void admit_locked();
   bool plan(TickBuf& B);
-  int enqueue(TickBuf& B);
+  int enqueue(TickBuf& B, const TickBuf& prev);
   int process(TickBuf& B);
   void finish(HostSlot& h, int status, double mean, double se, int64_t main_paths);
   void fail_all(int status);
@@ -267,16 +280,19 @@ int Server::init(const sdemc_server_cfg& c) {
   int64_t half = (cfg.mem_budget - fixed_bytes) / 2;
   if (half > ((int64_t)1 << 30)) half = (int64_t)1 << 30;
   part_cap = half / 8;
-  if ((rc = check_cuda(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "stream create"))) return rc;
-  side.resize(cfg.side_streams);
-  join.resize(cfg.side_streams);
-  for (int i = 0; i < cfg.side_streams; ++i) {
-    if ((rc = check_cuda(cudaStreamCreateWithFlags(&side[i], cudaStreamNonBlocking), "stream create"))) return rc;
-    if ((rc = check_cuda(cudaEventCreateWithFlags(&join[i], cudaEventDisableTiming), "event create"))) return rc;
-  }
-  if ((rc = check_cuda(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "event create"))) return rc;
   if ((rc = check_cuda(cudaMalloc(&slots_d, ms * sizeof(ServeSlot)), "slot table"))) return rc;
+  for (int i = 0; i < kStamps; ++i)
+    if ((rc = check_cuda(cudaEventCreate(&stamp[i]), "event create"))) return rc;
   for (TickBuf& B : buf) {
+    if ((rc = check_cuda(cudaStreamCreateWithFlags(&B.stream, cudaStreamNonBlocking), "stream create"))) return rc;
+    B.side.resize(cfg.side_streams);
+    B.join.resize(cfg.side_streams);
+    for (int i = 0; i < cfg.side_streams; ++i) {
+      if ((rc = check_cuda(cudaStreamCreateWithFlags(&B.side[i], cudaStreamNonBlocking), "stream create"))) return rc;
+      if ((rc = check_cuda(cudaEventCreateWithFlags(&B.join[i], cudaEventDisableTiming), "event create"))) return rc;
+    }
+    if ((rc = check_cuda(cudaEventCreateWithFlags(&B.fork, cudaEventDisableTiming), "event create"))) return rc;
+    if ((rc = check_cuda(cudaEventCreateWithFlags(&B.red_done, cudaEventDisableTiming), "event create"))) return rc;
     if ((rc = check_cuda(cudaMallocHost(&B.entries_h, ms * sizeof(ServeEntry)), "pinned entries"))) return rc;
     if ((rc = check_cuda(cudaMallocHost(&B.installs_h, ms * sizeof(ServeInstall)), "pinned installs"))) return rc;
     if ((rc = check_cuda(cudaMallocHost(&B.done_h, ms * sizeof(ServeDone)), "pinned done"))) return rc;
@@ -286,7 +302,6 @@ int Server::init(const sdemc_server_cfg& c) {
     if ((rc = check_cuda(cudaMalloc(&B.counters_d, kNumClassKeys * 8), "counters"))) return rc;
     if ((rc = check_cuda(cudaMalloc(&B.part_d, part_cap * 8), "tick partials"))) return rc;
     if ((rc = check_cuda(cudaEventCreate(&B.t0), "event create"))) return rc;
-    if ((rc = check_cuda(cudaEventCreate(&B.t1), "event create"))) return rc;
   }
   hs.assign(ms, HostSlot());
   free_slots.clear();
@@ -298,9 +313,16 @@ int Server::init(const sdemc_server_cfg& c) {
 }
 
 void Server::release() {
-  if (stream) cudaStreamSynchronize(stream);
-  for (cudaStream_t s : side) if (s) cudaStreamSynchronize(s);
   for (TickBuf& B : buf) {
+    if (B.stream) cudaStreamSynchronize(B.stream);
+    for (cudaStream_t s : B.side) if (s) cudaStreamSynchronize(s);
+  }
+  for (TickBuf& B : buf) {
+    for (cudaEvent_t e : B.join) if (e) cudaEventDestroy(e);
+    if (B.fork) cudaEventDestroy(B.fork);
+    if (B.red_done) cudaEventDestroy(B.red_done);
+    for (cudaStream_t s : B.side) if (s) cudaStreamDestroy(s);
+    if (B.stream) cudaStreamDestroy(B.stream);
     if (B.entries_h) cudaFreeHost(B.entries_h);
     if (B.installs_h) cudaFreeHost(B.installs_h);
     if (B.done_h) cudaFreeHost(B.done_h);
@@ -310,19 +332,14 @@ void Server::release() {
     if (B.counters_d) cudaFree(B.counters_d);
     if (B.part_d) cudaFree(B.part_d);
     if (B.t0) cudaEventDestroy(B.t0);
-    if (B.t1) cudaEventDestroy(B.t1);
     B = TickBuf();
   }
   if (slots_d) cudaFree(slots_d);
   slots_d = nullptr;
-  for (cudaEvent_t e : join) if (e) cudaEventDestroy(e);
-  join.clear();
-  if (fork) cudaEventDestroy(fork);
-  fork = nullptr;
-  for (cudaStream_t s : side) if (s) cudaStreamDestroy(s);
-  side.clear();
-  if (stream) cudaStreamDestroy(stream);
-  stream = nullptr;
+  for (cudaEvent_t& e : stamp) {
+    if (e) cudaEventDestroy(e);
+    e = nullptr;
+  }
 }
 
 // Pending requests -> free slots, in arrival order, while the budget allows.
@@ -423,6 +440,8 @@ bool Server::plan(TickBuf& B) {
     E.chunk_begin = chunk;
     E.nchunks = picks[i].nch;
     E.part_off = poff;
+    E.base = h.cursor;
+    E.end = h.phase_end;
     chunk += E.nchunks;
     poff += E.nchunks * E.width;
     h.cursor = std::min(h.cursor + E.nchunks * kChunk, h.phase_end);
@@ -441,8 +460,10 @@ bool Server::plan(TickBuf& B) {
   return true;
 }
 
-int Server::enqueue(TickBuf& B) {
+int Server::enqueue(TickBuf& B, const TickBuf& prev) {
   int rc;
+  cudaStream_t stream = B.stream;
+  B.seq = ticks_enqueued++;
   if ((rc = check_cuda(cudaEventRecord(B.t0, stream), "tick start"))) return rc;
   if (B.n_installs > 0 &&
       (rc = check_cuda(cudaMemcpyAsync(B.installs_d, B.installs_h, B.n_installs * sizeof(ServeInstall),
@@ -452,16 +473,18 @@ int Server::enqueue(TickBuf& B) {
       (rc = check_cuda(cudaMemcpyAsync(B.entries_d, B.entries_h, B.n_entries * sizeof(ServeEntry),
                                        cudaMemcpyHostToDevice, stream), "plan upload")))
     return rc;
+  // installs touch only slots that no tick in flight has entries for (new
+  // requests, and slots whose previous phase ended in a tick already processed)
   if ((rc = launch_serve_install(slots_d, B.installs_d, B.n_installs, B.counters_d, kNumClassKeys, stream)))
     return rc;
-  const int nside = (int)side.size();
+  const int nside = (int)B.side.size();
   if (nside > 0) {
-    if ((rc = check_cuda(cudaEventRecord(fork, stream), "fork record"))) return rc;
+    if ((rc = check_cuda(cudaEventRecord(B.fork, stream), "fork record"))) return rc;
     for (int j = 0; j < nside; ++j)
-      if ((rc = check_cuda(cudaStreamWaitEvent(side[j], fork, 0), "fork wait"))) return rc;
+      if ((rc = check_cuda(cudaStreamWaitEvent(B.side[j], B.fork, 0), "fork wait"))) return rc;
   }
   int k = 0, launched = 0;
-  while (k < B.n_entries) {
+  while (k < B.n_entries && rc == SDEMC_OK) {
     const ServeEntry& E0 = B.entries_h[k];
     const sdemc_inst& I = hs[E0.slot].req.inst;
     const int key = class_key(E0.kind, I);
@@ -477,28 +500,32 @@ int Server::enqueue(TickBuf& B) {
     P.counter = B.counters_d + key;
     P.part = B.part_d;
     const int64_t chunks = P.chunk_end - P.chunk_begin;
-    cudaStream_t ks = nside > 0 ? side[launched % nside] : stream;
+    cudaStream_t ks = nside > 0 ? B.side[launched % nside] : stream;
     if (E0.kind == kKindPlain)
       rc = launch_serve_plain(I.dim, I.noise, loop_mode_of(I), P, threads, chunks, ks);
     else
       rc = launch_serve_cv(E0.kind, I.dim, P, threads, chunks, ks);
-    if (rc) return rc;
     ++launched;
     k = j;
   }
   B.launches = launched + 1 + (B.n_entries > 0 ? 1 : 0);
-  if (nside > 0) {
-    for (int j = 0; j < nside; ++j) {
-      if ((rc = check_cuda(cudaEventRecord(join[j], side[j]), "join record"))) return rc;
-      if ((rc = check_cuda(cudaStreamWaitEvent(stream, join[j], 0), "join wait"))) return rc;
-    }
+  // join the side streams back even after a failed launch
+  for (int j = 0; j < nside; ++j) {
+    int jr = check_cuda(cudaEventRecord(B.join[j], B.side[j]), "join record");
+    if (jr == SDEMC_OK) jr = check_cuda(cudaStreamWaitEvent(stream, B.join[j], 0), "join wait");
+    if (rc == SDEMC_OK) rc = jr;
   }
+  if (rc) return rc;
+  // each slot's sums are folded tick after tick: this reduction follows the
+  // previous tick's (a never-recorded event is already complete)
+  if ((rc = check_cuda(cudaStreamWaitEvent(stream, prev.red_done, 0), "reduce order"))) return rc;
   if ((rc = launch_serve_reduce(slots_d, B.entries_d, B.n_entries, B.part_d, B.done_d, stream))) return rc;
+  if ((rc = check_cuda(cudaEventRecord(B.red_done, stream), "reduce done"))) return rc;
   if (B.n_done > 0 &&
       (rc = check_cuda(cudaMemcpyAsync(B.done_h, B.done_d, B.n_done * sizeof(ServeDone), cudaMemcpyDeviceToHost,
                                        stream), "done readback")))
     return rc;
-  return check_cuda(cudaEventRecord(B.t1, stream), "tick end");
+  return check_cuda(cudaEventRecord(stamp[B.seq % kStamps], stream), "tick end");
 }
 
 void Server::finish(HostSlot& h, int status, double mean, double se, int64_t main_paths) {
@@ -531,14 +558,29 @@ void Server::finish(HostSlot& h, int status, double mean, double se, int64_t mai
 }
 
 int Server::process(TickBuf& B) {
-  int rc = check_cuda(cudaEventSynchronize(B.t1), "tick wait");
+  cudaEvent_t t_end = stamp[B.seq % kStamps];
+  int rc = check_cuda(cudaEventSynchronize(t_end), "tick wait");
   if (rc) return rc;
   float ms = 0.f;
-  cudaEventElapsedTime(&ms, B.t0, B.t1);
+  cudaEventElapsedTime(&ms, B.t0, t_end);
+  // place the tick on one device timeline: its end relative to the previous
+  // processed tick's end (both stamps still recorded: the ring outlives the
+  // two ticks in flight), its start by its own duration; busy time is the
+  // union of the tick intervals (ticks overlap)
+  double end_ms = 0.0;
+  if (B.seq > 0) {
+    float gap = 0.f;
+    cudaEventElapsedTime(&gap, stamp[(B.seq - 1) % kStamps], t_end);
+    end_ms = end_prev_ms + (double)gap;
+  }
+  const double start_ms = end_ms - (double)ms;
+  const double added = std::max(0.0, end_ms - std::max(start_ms, B.seq > 0 ? last_end_ms : start_ms));
+  end_prev_ms = end_ms;
+  last_end_ms = B.seq > 0 ? std::max(last_end_ms, end_ms) : end_ms;
   {
     std::lock_guard<std::mutex> lk(mu);
     st.ticks++;
-    st.busy_s += ms * 1e-3;
+    st.busy_s += added * 1e-3;
     int b = 0;
     for (double edge = 0.125; b < 15 && ms >= edge; edge *= 2.0) ++b;
     st.tick_hist[b]++;
@@ -673,7 +715,7 @@ void Server::loop() {
     TickBuf& B = buf[next];
     bool launched = false;
     if (plan(B)) {
-      if (enqueue(B) != SDEMC_OK) {
+      if (enqueue(B, buf[next ^ 1]) != SDEMC_OK) {
         fail_all(SDEMC_ECUDA);
         break;
       }
@@ -700,7 +742,7 @@ void Server::loop() {
     // idle: sleep until a request arrives (admission runs at the top)
     if (!runnable) cv_in.wait_for(lk, std::chrono::milliseconds(2));
   }
-  if (inflight >= 0) cudaEventSynchronize(buf[inflight].t1);
+  if (inflight >= 0) cudaEventSynchronize(stamp[buf[inflight].seq % kStamps]);
 }
 
 }  // namespace sdemc

@@ -72,6 +72,7 @@ struct ServeEntry {
   int64_t chunk_begin;  // global chunk index of the entry's first chunk in the tick
   int64_t nchunks;
   int64_t part_off;     // offset (doubles) of its chunk partials
+  int64_t base, end;    // the slice's first local path and the end of its phase
 };
 
 struct ServeDone {
@@ -222,8 +223,11 @@ serve_kernel(const __grid_constant__ ServeParams P) {
       part_off = E.part_off;
       slot = E.slot;
       const ServeSlot& S = P.slots[slot];
-      base = S.st.cursor;
-      end = S.st.phase_end;
+      // the slice's bounds come with the entry: a class kernel reads only the
+      // slot's descriptor and coefficients, which no running tick writes, so
+      // it may overlap the previous tick's kernels and reduction
+      base = E.base;
+      end = E.end;
       __syncwarp();
       const uint32_t* src = reinterpret_cast<const uint32_t*>(&S.inst);
       uint32_t* dst = reinterpret_cast<uint32_t*>(&s_inst[wid]);
