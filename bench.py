@@ -64,8 +64,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--plain-windows", type=int, default=10,
                     help="windows of the stream the plain one-request-per-launch server replays")
-    ap.add_argument("--sections", default="rainbow,materialise,mlmc,mix,cv,accuracy",
-                    help="extra sections measured once: rainbow, materialise, mlmc, mix, cv, accuracy "
+    ap.add_argument("--sections", default="rainbow,materialise,mlmc,mix,cv,cvserved,accuracy",
+                    help="extra sections measured once: rainbow, materialise, mlmc, mix, cv, cvserved, accuracy "
                          "(comma list, or 'none')")
     ap.add_argument("--profile-store", type=int, default=0,
                     help="profiling driver: materialise this many 2D rainbow paths (K4, AdaptedPathData "
@@ -656,6 +656,77 @@ def bench_cv_learned(dev, epochs=10):
                     "simulates the paths inside the same kernel (nothing materialised)"}
 
 
+def bench_cv_learned_served(dev, n_requests=24, epochs=4):
+    """The learned control variate on the served stream's requests with d <= 2
+    (the dimensions the network form covers), one request at a time through
+    the reference's run_cv_mc flow (sde_mc/mc.py:443-467): train
+    Mlp(1 + d, [64, 64, 64], d) on the request's pilot paths (K4 + K5/K6),
+    size the main run for a 95% half-width of target x |price| from a
+    control-variate pilot of the same size on fresh paths, then price the main
+    run with K7.  Reported beside the served regression control variate and
+    the plain estimator on the same requests (device time to the target)."""
+    import numpy as np
+    import torch
+    import sde_mc_gb300 as sm
+    from sde_mc_gb300 import kernels as K
+    from sde_mc_gb300 import serve
+    from sde_mc_gb300 import stream as S
+    reqs = [r for r in S.make_stream(RATE, 1.0, seed=1) if r.dim <= 2][:n_requests]
+    rows = []
+    for r in reqs:
+        m = r.instance()
+        solver, payoff, disc, d = m.solver, m.payoff, m.discounter, m.dim
+        torch.manual_seed(r.idx)
+        f = sm.Mlp(1 + d, [64, 64, 64], d, batch_norm=False, batch_norm_init=False)
+        opt = torch.optim.Adam(f.parameters(), lr=1e-3)
+        models = [f, sm.ZeroFunction(d)]
+        n0 = int(r.inst.num_paths)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dl = sm.simulate_adapted_data(n0, solver, payoff, disc, bs=min(4096, n0))
+        sm.train_adapted_control_variates(models, opt, dl, solver, disc, epochs=epochs, print_losses=False)
+        del dl
+        pilot = sm.mc_apply_cvs(models, solver, n0, payoff, disc)
+        sd = pilot.sample_std * math.sqrt(n0)
+        n = max(64, int(math.ceil((1.96 * sd / (r.target * abs(pilot.sample_mean))) ** 2)))
+        st = sm.mc_apply_cvs(models, solver, n, payoff, disc)
+        torch.cuda.synchronize()
+        t_cv = time.perf_counter() - t0
+        # the plain estimator on the same request: its pilot variance sizes its main run
+        pl = K.price(r.phase(n0, 1 << 40)).cpu().tolist()
+        n_plain = max(64, int(math.ceil(1.96 ** 2 * pl[4] / (r.target * abs(pl[3])) ** 2)))
+        rows.append({"idx": r.idx, "dim": d, "target": r.target, "pilot_paths": n0, "main_paths": n,
+                     "vrf": pl[4] / max(sd * sd, 1e-300), "service_s": t_cv, "mean": st.sample_mean,
+                     "plain_main_paths": n_plain})
+    # the served regression control variate on the same requests, alone in a server
+    with serve.Server(max_slots=64, mem_budget=4 << 30, device=dev) as srv:
+        t0 = time.perf_counter()
+        for r in reqs:
+            srv.submit_inst(r.inst, r.target, estimator="linear_cv", tag=r.idx)
+        res = {x.tag: x for x in srv.wait(len(reqs))}
+        t_reg = time.perf_counter() - t0
+        busy = srv.stats()["busy_s"]
+    for row in rows:
+        x = res[row["idx"]]
+        row.update(regression_vrf=x.vrf, regression_main_paths=x.main_paths,
+                   regression_vs_learned_in_se=(x.mean - row["mean"]) / max(x.se, 1e-300))
+    svc = np.asarray([row["service_s"] for row in rows])
+    return {"workload": "the served stream's first %d requests with d <= 2 (the network form's dimensions)" % len(rows),
+            "form": "learned CV per request: train on the pilot paths (%d epochs, Adam lr 1e-3, batch 4096), "
+                    "CV pilot on fresh paths, main run with K7" % epochs,
+            "requests": len(rows), "learned_prices_per_s": len(rows) / float(svc.sum()),
+            "learned_service_p50_ms": float(np.percentile(svc, 50) * 1e3),
+            "learned_service_p99_ms": float(np.percentile(svc, 99) * 1e3),
+            "learned_vrf_median": float(np.median([row["vrf"] for row in rows])),
+            "regression_prices_per_s_busy": len(rows) / busy, "regression_wall_s": t_reg,
+            "regression_vrf_median": float(np.median([row["regression_vrf"] for row in rows])),
+            "main_paths_learned_over_regression": float(np.median([row["main_paths"] / max(row["regression_main_paths"], 1)
+                                                                   for row in rows])),
+            "rows": rows,
+            "note": "a network is trained per request (the reference's learned CV has no form shared across "
+                    "instances), so its cost is the training, not the main run"}
+
+
 def _err(mean, se, ref, ref_se):
     e = mean - ref
     return {"price": mean, "err": e, "rel_err": e / ref, "err_in_se": e / math.hypot(se, ref_se)}
@@ -990,6 +1061,8 @@ def main():
             line["batched_mix"] = _section(bench_batched_mix, 5, 3)
         if "cv" in secs:
             line["cv_learned"] = _section(bench_cv_learned, dev)
+        if "cvserved" in secs:
+            line["cv_learned_served"] = _section(bench_cv_learned_served, dev)
         if "accuracy" in secs:
             line["accuracy"] = _section(bench_accuracy, dev, line, b)
         threads = os.cpu_count() or 1

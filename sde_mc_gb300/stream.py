@@ -32,13 +32,20 @@ TARGETS = (1e-2, 3e-3, 1e-3)
 
 class StreamRequest:
     """One request: arrival time ``t`` (s), its pilot descriptor ``inst``
-    (num_paths = pilot paths, stream_id = idx) and its relative target."""
+    (num_paths = pilot paths, stream_id = idx), its relative target and the
+    mix-law parameters it was drawn with (``params``, as
+    workloads.basket_instance takes them)."""
 
-    __slots__ = ("idx", "t", "inst", "target", "dim", "steps", "rate")
+    __slots__ = ("idx", "t", "inst", "target", "dim", "steps", "rate", "params")
 
-    def __init__(self, idx, t, inst, target):
+    def __init__(self, idx, t, inst, target, params=None):
         self.idx, self.t, self.inst, self.target = idx, float(t), inst, float(target)
         self.dim, self.steps, self.rate = int(inst.dim), int(inst.num_steps), float(inst.rate)
+        self.params = params
+
+    def instance(self, device="cuda"):
+        """The request's model objects (a workloads.MixInstance)."""
+        return workloads.basket_instance(self.idx, *self.params, device=device)
 
     def phase(self, num_paths, path_offset):
         """Descriptor of num_paths paths starting at local index path_offset."""
@@ -69,7 +76,7 @@ def make_stream(rate=2000.0, seconds=60.0, seed=1, t_begin=0.0):
         if t >= t_begin:
             m = workloads.basket_instance(idx, *params)
             inst = lower(m.solver, m.payoff, m.discounter, num_paths=m.paths, path_offset=0, stream_id=idx)
-            out.append(StreamRequest(idx, t - t_begin, inst, target))
+            out.append(StreamRequest(idx, t - t_begin, inst, target, params))
         idx += 1
     return out
 
