@@ -3,7 +3,7 @@
 // One host thread per server drives the device in ticks.  Each tick it
 //   1. admits queued requests into free slots while the memory budget allows
 //      (a request reserves its slot record and the chunk partials of its
-//      largest slice in both tick buffers);
+//      largest slice in every tick buffer);
 //   2. plans the tick: every scheduled slot contributes one slice of its
 //      current phase (min(slice, remaining) paths; the slice size is a
 //      function of the request alone), in FIFO or shortest-remaining order up
@@ -15,9 +15,10 @@
 //      finished phases: a pilot sizes the main run (find_num_trials,
 //      sde_mc/mc.py:418-427) and fits the control-variate coefficients; a
 //      main run becomes a result.
-// Two tick buffers alternate, each with its own stream and side streams, so
-// the next tick is queued before the running one ends and its class kernels
-// start while the running tick's last kernels drain: a class kernel reads only
+// kTickBufs tick buffers rotate, each with its own stream and side streams,
+// so up to kTickBufs ticks are in flight: the next ticks are queued before the
+// running one ends and their class kernels start while the running tick's
+// last kernels drain: a class kernel reads only
 // its entries and the slots' descriptors and coefficients (no running tick
 // writes those), and the one ordering across ticks — each slot's FP64 sums are
 // folded tick after tick — is kept by making each tick's reduction wait for
@@ -50,6 +51,7 @@ constexpr int kNumClassKeys = kNumKinds * 3 * 2 * SDEMC_MAX_DIM;
 constexpr int64_t kMaxSlicePaths = 1 << 18;
 constexpr int64_t kMinSlicePaths = 1 << 10;
 constexpr double kZ95 = 1.96;
+constexpr int kTickBufs = 3;  // ticks in flight at most
 
 bool lcv_supported(const sdemc_inst& I) {
   return I.noise == SDEMC_NOISE_DIAG && !(I.flags & SDEMC_INST_PAYOFF_AT_NOMINAL_STEP);
@@ -223,10 +225,10 @@ struct Server {
   int64_t part_cap = 0;  // doubles per tick buffer
   int64_t fixed_bytes = 0;
   ServeSlot* slots_d = nullptr;
-  TickBuf buf[2];
-  // tick-end stamps: a ring longer than the two ticks in flight, so the
-  // previous tick's end is still recorded when a tick is processed
-  static constexpr int kStamps = 4;
+  TickBuf buf[kTickBufs];
+  // tick-end stamps: a ring longer than the ticks in flight, so the previous
+  // tick's end is still recorded when a tick is processed
+  static constexpr int kStamps = 2 * kTickBufs + 2;
   cudaEvent_t stamp[kStamps] = {};
   int64_t ticks_enqueued = 0;
   double end_prev_ms = 0.0, last_end_ms = 0.0;  // device timeline of processed ticks
@@ -271,15 +273,15 @@ int Server::init(const sdemc_server_cfg& c) {
   if (rc) return rc;
   const int64_t ms = cfg.max_slots;
   fixed_bytes = ms * (int64_t)sizeof(ServeSlot) +
-                2 * (ms * (int64_t)(sizeof(ServeEntry) + sizeof(ServeInstall) + sizeof(ServeDone)) +
+                kTickBufs * (ms * (int64_t)(sizeof(ServeEntry) + sizeof(ServeInstall) + sizeof(ServeDone)) +
                      kNumClassKeys * 8);
-  const int64_t min_part = 2 * (kMaxSlicePaths / kChunk) * kServeMaxW * 8;
+  const int64_t min_part = kTickBufs * (kMaxSlicePaths / kChunk) * kServeMaxW * 8;
   if (cfg.mem_budget < fixed_bytes + min_part)
     return fail(SDEMC_ENOMEM, "mem_budget %lld below the %lld bytes of slot tables and one full slice",
                 (long long)cfg.mem_budget, (long long)(fixed_bytes + min_part));
-  int64_t half = (cfg.mem_budget - fixed_bytes) / 2;
-  if (half > ((int64_t)1 << 30)) half = (int64_t)1 << 30;
-  part_cap = half / 8;
+  int64_t share = (cfg.mem_budget - fixed_bytes) / kTickBufs;
+  if (share > ((int64_t)1 << 30)) share = (int64_t)1 << 30;
+  part_cap = share / 8;
   if ((rc = check_cuda(cudaMalloc(&slots_d, ms * sizeof(ServeSlot)), "slot table"))) return rc;
   for (int i = 0; i < kStamps; ++i)
     if ((rc = check_cuda(cudaEventCreate(&stamp[i]), "event create"))) return rc;
@@ -353,7 +355,7 @@ void Server::admit_locked() {
     slice = std::min(std::max(slice, kMinSlicePaths), kMaxSlicePaths);
     slice = (slice + kChunk - 1) / kChunk * kChunk;
     const int wmax = lcv ? pilot_width(I.dim) : 3;
-    const int64_t reserve = (int64_t)sizeof(ServeSlot) + 2 * (slice / kChunk) * wmax * 8;
+    const int64_t reserve = (int64_t)sizeof(ServeSlot) + kTickBufs * (slice / kChunk) * wmax * 8;
     if (st.mem_in_use + reserve > cfg.mem_budget) break;
     const int s = free_slots.back();
     free_slots.pop_back();
@@ -704,35 +706,48 @@ void Server::loop() {
     fail_all(SDEMC_ECUDA);
     return;
   }
-  int inflight = -1;
-  int next = 0;
+  // buffers in flight: oldest, oldest + 1, ... (count of them), in tick order
+  int oldest = 0, count = 0;
   for (;;) {
     {
       std::lock_guard<std::mutex> lk(mu);
       if (stop) break;
       admit_locked();
     }
-    TickBuf& B = buf[next];
     bool launched = false;
-    if (plan(B)) {
-      if (enqueue(B, buf[next ^ 1]) != SDEMC_OK) {
-        fail_all(SDEMC_ECUDA);
+    if (count < kTickBufs) {
+      const int next = (oldest + count) % kTickBufs;
+      TickBuf& B = buf[next];
+      if (plan(B)) {
+        if (enqueue(B, buf[(next + kTickBufs - 1) % kTickBufs]) != SDEMC_OK) {
+          fail_all(SDEMC_ECUDA);
+          break;
+        }
+        launched = true;
+        ++count;
+      }
+    }
+    // handle finished ticks in order; block on the oldest only when every
+    // buffer is in flight or there was nothing new to launch
+    bool failed = false;
+    while (count > 0) {
+      const cudaError_t q = cudaEventQuery(stamp[buf[oldest].seq % kStamps]);
+      if (q == cudaErrorNotReady) (void)cudaGetLastError();  // not an error: the tick still runs
+      const bool done = q == cudaSuccess;
+      if (!done && launched && count < kTickBufs) break;
+      if (process(buf[oldest]) != SDEMC_OK) {
+        failed = true;
         break;
       }
-      launched = true;
+      oldest = (oldest + 1) % kTickBufs;
+      --count;
+      if (!done) break;  // waited once: plan again before waiting more
     }
-    if (inflight >= 0) {
-      if (process(buf[inflight]) != SDEMC_OK) {
-        fail_all(SDEMC_ECUDA);
-        break;
-      }
-      inflight = -1;
+    if (failed) {
+      fail_all(SDEMC_ECUDA);
+      break;
     }
-    if (launched) {
-      inflight = next;
-      next ^= 1;
-      continue;
-    }
+    if (launched || count > 0) continue;
     if (!staged.empty()) continue;
     std::unique_lock<std::mutex> lk(mu);
     if (stop) break;
@@ -742,7 +757,7 @@ void Server::loop() {
     // idle: sleep until a request arrives (admission runs at the top)
     if (!runnable) cv_in.wait_for(lk, std::chrono::milliseconds(2));
   }
-  if (inflight >= 0) cudaEventSynchronize(stamp[buf[inflight].seq % kStamps]);
+  for (int i = 0; i < count; ++i) cudaEventSynchronize(stamp[buf[(oldest + i) % kTickBufs].seq % kStamps]);
 }
 
 }  // namespace sdemc
