@@ -126,6 +126,9 @@ typedef struct sdemc_inst {
   float payoff_scale;   /* Option.discount                                  */
   float discount;       /* discounter(T) as float32                         */
   float disc_rate;      /* ConstantShortRate.r (for per-step discounting)   */
+  int32_t reserved0[2]; /* zero; the arrays below start on 16-byte boundaries,
+                           so kernels that stage the descriptor in shared
+                           memory read them with vector loads             */
   float x0[SDEMC_MAX_DIM];
   float drift_a[SDEMC_MAX_DIM], drift_b[SDEMC_MAX_DIM];
   float diff_s[SDEMC_MAX_DIM], diff_q[SDEMC_MAX_DIM];

@@ -45,7 +45,7 @@ class SdemcInst(ctypes.Structure):
         ("seed", ctypes.c_uint64), ("path_offset", ctypes.c_uint64), ("num_paths", ctypes.c_int64),
         ("T", ctypes.c_float), ("h", ctypes.c_float), ("rate", ctypes.c_float),
         ("inv_rate", ctypes.c_float), ("strike", ctypes.c_float), ("payoff_scale", ctypes.c_float),
-        ("discount", ctypes.c_float), ("disc_rate", ctypes.c_float),
+        ("discount", ctypes.c_float), ("disc_rate", ctypes.c_float), ("reserved0", ctypes.c_int32 * 2),
         ("x0", _f8), ("drift_a", _f8), ("drift_b", _f8), ("diff_s", _f8), ("diff_q", _f8),
         ("diff2_s", _f8), ("diff2_q", _f8), ("jump_g", _f8), ("jump_k", _f8), ("jump_cdf", _f8),
         ("chol", ctypes.c_float * CHOL_LEN), ("mark_p", ctypes.c_float * MARK_PARAMS),

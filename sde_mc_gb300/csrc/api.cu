@@ -215,6 +215,8 @@ extern "C" int sdemc_fp32_probe(int iters, float* d_sink, int sink_len, double* 
 extern "C" {
 
 int sdemc_abi_version(void) { return SDEMC_ABI_VERSION; }
+static_assert(offsetof(sdemc_inst, x0) % 16 == 0 && sizeof(sdemc_inst) % 16 == 0,
+              "the descriptor's arrays start on 16-byte boundaries");
 size_t sdemc_inst_size(void) { return sizeof(sdemc_inst); }
 
 int sdemc_inst_offsets(size_t* h_offsets, int* n) {
@@ -226,7 +228,8 @@ int sdemc_inst_offsets(size_t* h_offsets, int* n) {
       offsetof(sdemc_inst, seed), offsetof(sdemc_inst, path_offset), offsetof(sdemc_inst, num_paths),
       offsetof(sdemc_inst, T), offsetof(sdemc_inst, h), offsetof(sdemc_inst, rate),
       offsetof(sdemc_inst, inv_rate), offsetof(sdemc_inst, strike), offsetof(sdemc_inst, payoff_scale),
-      offsetof(sdemc_inst, discount), offsetof(sdemc_inst, disc_rate), offsetof(sdemc_inst, x0),
+      offsetof(sdemc_inst, discount), offsetof(sdemc_inst, disc_rate), offsetof(sdemc_inst, reserved0),
+      offsetof(sdemc_inst, x0),
       offsetof(sdemc_inst, drift_a), offsetof(sdemc_inst, drift_b), offsetof(sdemc_inst, diff_s),
       offsetof(sdemc_inst, diff_q), offsetof(sdemc_inst, diff2_s), offsetof(sdemc_inst, diff2_q),
       offsetof(sdemc_inst, jump_g), offsetof(sdemc_inst, jump_k), offsetof(sdemc_inst, jump_cdf),

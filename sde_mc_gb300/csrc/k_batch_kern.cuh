@@ -68,7 +68,7 @@ SDEMC_DI void batch_emit(const BatchParams& B, const sdemc_inst& I, const float*
 template <int D, int NOISE, int MODE, int PATHS>
 __global__ void __launch_bounds__(256)
 batch_kernel(const __grid_constant__ BatchParams B) {
-  __shared__ sdemc_inst s_inst[kBatchMaxWarps];
+  __shared__ __align__(16) sdemc_inst s_inst[kBatchMaxWarps];  // 16-byte aligned arrays: vector loads
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int cur = -1;
   int64_t lo = 0, hi = 0;

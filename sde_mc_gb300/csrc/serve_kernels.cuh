@@ -193,7 +193,7 @@ struct DeltaCvSink {
 template <int D, int NOISE, int MODE, int KIND>
 __global__ void __launch_bounds__(256, 3)
 serve_kernel(const __grid_constant__ ServeParams P) {
-  __shared__ sdemc_inst s_inst[kServeMaxWarps];
+  __shared__ __align__(16) sdemc_inst s_inst[kServeMaxWarps];  // 16-byte aligned arrays: vector loads
   __shared__ float s_beta[kServeMaxWarps][2 * D + 1];
   __shared__ CvWeights s_cw[kServeMaxWarps];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
