@@ -276,7 +276,10 @@ int sdemc_price_noalloc(const sdemc_inst* h_inst, const sdemc_cfg* h_cfg,
  * sdemc_batch_scratch_bytes(h_blob)) must be zeroed before its first use.
  * h_cfgs (nullable) holds one launch configuration per class in class order;
  * side_streams (nullable, n_side entries) lets class kernels overlap; the
- * calls on them are joined back into `stream` before the reduction.         */
+ * calls on them are joined back into `stream` before the reduction.  A class
+ * whose instances share one seed gets its Philox round keys from h_blob at
+ * launch as kernel arguments (a captured launch keeps them): edit path
+ * offsets in place between replays, but plan again to change seeds.         */
 typedef struct sdemc_batch_class {
   int32_t dim, noise, mode, count;  /* mode: bit 0 exact Euler, bit 1 nominal */
   int32_t first;                    /* first instance (plan order)            */

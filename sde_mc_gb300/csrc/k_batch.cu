@@ -279,6 +279,11 @@ extern "C" int sdemc_price_batch(const void* h_blob, const void* d_blob, void* d
     B.counter = reinterpret_cast<unsigned long long*>(sc + S.counters) + k;
     B.status = reinterpret_cast<int32_t*>(sc + S.status);
     B.part = reinterpret_cast<double*>(sc + S.part);
+    const sdemc_inst* hinsts = reinterpret_cast<const sdemc_inst*>(hb + H.off_insts);
+    B.uniform_seed = 1;
+    for (int i = C.first + 1; i < C.first + C.count; ++i)
+      if (hinsts[i].seed != hinsts[C.first].seed) { B.uniform_seed = 0; break; }
+    if (B.uniform_seed && C.count > 0) B.rk = make_round_keys(hinsts[C.first].seed);
     const int64_t chunks = C.chunk_end - C.chunk_begin;
     if (chunks == 0) continue;
     cudaStream_t ks = n_side > 0 ? (cudaStream_t)side_streams[k % n_side] : s;

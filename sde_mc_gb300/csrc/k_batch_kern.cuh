@@ -19,7 +19,19 @@ struct BatchParams {
   unsigned long long* counter;   // this class's chunk counter
   int32_t* status;               // per instance (plan order)
   double* part;                  // chunk partials, 3 doubles per global chunk
+  // when every instance of the class has the same seed, the Philox round keys
+  // are launch constants (as in K1); otherwise each warp derives them
+  int32_t uniform_seed;
+  RoundKeys rk;
 };
+
+template <class KS> SDEMC_DI KS batch_keys(const BatchParams& B, const sdemc_inst& I);
+template <> SDEMC_DI SeedKeys batch_keys<SeedKeys>(const BatchParams&, const sdemc_inst& I) {
+  return SeedKeys{(uint32_t)I.seed, (uint32_t)(I.seed >> 32)};
+}
+template <> SDEMC_DI ConstKeys batch_keys<ConstKeys>(const BatchParams& B, const sdemc_inst&) {
+  return ConstKeys{&B.rk};
+}
 
 // Find the instance of global chunk gc (binary search on the chunk prefix),
 // stage its descriptor in shared memory and flush the previous instance's
@@ -65,7 +77,7 @@ SDEMC_DI void batch_emit(const BatchParams& B, const sdemc_inst& I, const float*
 // chunks; when both belong to one instance they step together (simulate2),
 // otherwise one after the other.  Either way every chunk's bits are those of
 // the one-path loop.
-template <int D, int NOISE, int MODE, int PATHS>
+template <int D, int NOISE, int MODE, int PATHS, class KS>
 __global__ void __launch_bounds__(256)
 batch_kernel(const __grid_constant__ BatchParams B) {
   __shared__ __align__(16) sdemc_inst s_inst[kBatchMaxWarps];  // 16-byte aligned arrays: vector loads
@@ -82,10 +94,10 @@ batch_kernel(const __grid_constant__ BatchParams B) {
     if (gc >= B.chunk_end) break;
     if (gc < lo || gc >= hi) stage_instance(B, gc, &s_inst[wid], cur, lo, hi, max_iters, ovf);
     const sdemc_inst& I = s_inst[wid];
-    const SeedKeys keys{(uint32_t)I.seed, (uint32_t)(I.seed >> 32)};
+    const KS keys = batch_keys<KS>(B, I);
     const int64_t p = (gc - lo) * kChunk + lane;
     if (PATHS == 2 && gc + 1 < hi) {
-      NativeDraws<D, NOISE, SeedKeys> da, db;
+      NativeDraws<D, NOISE, KS> da, db;
       da.init(I, (uint64_t)p, keys);
       db.init(I, (uint64_t)(p + kChunk), keys);
       float xa[D], xb[D];
@@ -95,7 +107,7 @@ batch_kernel(const __grid_constant__ BatchParams B) {
       continue;
     }
     {
-      NativeDraws<D, NOISE, SeedKeys> dr;
+      NativeDraws<D, NOISE, KS> dr;
       dr.init(I, (uint64_t)p, keys);
       NullSink sk;
       float x[D];
@@ -107,8 +119,8 @@ batch_kernel(const __grid_constant__ BatchParams B) {
       stage_instance(B, gc1, &s_inst[wid], cur, lo, hi, max_iters, ovf);
       const sdemc_inst& J = s_inst[wid];
       const int64_t p1 = (gc1 - lo) * kChunk + lane;
-      NativeDraws<D, NOISE, SeedKeys> dr;
-      dr.init(J, (uint64_t)p1, SeedKeys{(uint32_t)J.seed, (uint32_t)(J.seed >> 32)});
+      NativeDraws<D, NOISE, KS> dr;
+      dr.init(J, (uint64_t)p1, batch_keys<KS>(B, J));
       NullSink sk;
       float x[D];
       simulate<D, NOISE, MODE>(J, dr, sk, x, max_iters, ovf);
@@ -121,7 +133,8 @@ batch_kernel(const __grid_constant__ BatchParams B) {
 template <int D, int NOISE, int MODE>
 int launch_batch_t(const BatchParams& B, const sdemc_cfg* cfg, int64_t chunks, cudaStream_t s) {
   const int paths = cfg && cfg->interleave == 2 ? 2 : 1;
-  auto kern = paths == 2 ? batch_kernel<D, NOISE, MODE, 2> : batch_kernel<D, NOISE, MODE, 1>;
+  auto kern = B.uniform_seed ? (paths == 2 ? batch_kernel<D, NOISE, MODE, 2, ConstKeys> : batch_kernel<D, NOISE, MODE, 1, ConstKeys>)
+                             : (paths == 2 ? batch_kernel<D, NOISE, MODE, 2, SeedKeys> : batch_kernel<D, NOISE, MODE, 1, SeedKeys>);
   int threads = cfg && cfg->block_threads > 0 ? cfg->block_threads : 128;
   int per_sm = 0;
   int rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0), "occupancy query");
