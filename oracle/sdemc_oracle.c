@@ -143,17 +143,38 @@ static void native_fill4(const draws_t* d, uint32_t b, float* o) {
   o[0] = r0 * cosf(a0); o[1] = r0 * sinf(a0); o[2] = r1 * cosf(a1); o[3] = r1 * sinf(a1);
 }
 
+/* Normals of step k (called for k = 0, 1, 2, ... in turn), as the kernels
+ * draw them: for ZD in {1, 2, 3, 5, 6} the path's diffusion stream read
+ * densely, step k taking normals k ZD .. k ZD + ZD - 1, four per Philox block
+ * (the unused tail of a step's last block kept in d->buf for the next step);
+ * for ZD = 4, 7, 8 whole blocks per step, the first ZD normals used. */
 static void native_normals(draws_t* d, int ZD, int k, float* z) {
   if (ZD == 1 || ZD == 2) {
     int pos = (k * ZD) & 3;
     if (pos == 0) native_fill4(d, (uint32_t)((k * ZD) >> 2), d->buf);
     for (int i = 0; i < ZD; ++i) z[i] = d->buf[pos + i];
-  } else {
+  } else if (ZD % 4 == 0 || ZD == 7) {
     int nb = (ZD + 3) / 4;
     for (int b = 0; b < nb; ++b) {
       float o[4];
       native_fill4(d, (uint32_t)(k * nb + b), o);
       for (int q = 0; q < 4; ++q) if (4 * b + q < ZD) z[4 * b + q] = o[q];
+    }
+  } else {
+    const int off = (k * ZD) & 3, nc = off ? 4 - off : 0, take = nc < ZD ? nc : ZD;
+    float carry[4];
+    memcpy(carry, d->buf, sizeof(carry));
+    for (int j = 0; j < take; ++j) z[j] = carry[j];
+    const uint32_t b0 = (uint32_t)((k * ZD + take) >> 2);
+    const int nblk = (ZD - take + 3) / 4;
+    for (int nb = 0; nb < nblk; ++nb) {
+      float o[4];
+      native_fill4(d, b0 + (uint32_t)nb, o);
+      for (int q = 0; q < 4; ++q) {
+        const int idx = take + 4 * nb + q;
+        if (idx < ZD) z[idx] = o[q];
+        else d->buf[idx - ZD] = o[q];
+      }
     }
   }
 }

@@ -45,6 +45,31 @@ struct DrawsF64 {
     sincos(a1, &s1, &c1);
     o[0] = r0 * c0; o[1] = r0 * s0; o[2] = r1 * c1; o[3] = r1 * s1;
   }
+  // the dense schedule of NativeDraws::dense_step: the previous step's unused
+  // normals first, then new blocks, the last block's tail carried
+  template <int O>
+  __device__ void dense_step(int k, double* z) {
+    constexpr int NC = O == 0 ? 0 : 4 - O;
+    constexpr int TAKE = NC < D ? NC : D;
+    constexpr int NBLK = (D - TAKE + 3) / 4;
+    double carry[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) carry[j] = buf[j];
+#pragma unroll
+    for (int j = 0; j < TAKE; ++j) z[j] = carry[j];
+    const uint32_t b0 = (uint32_t)((k * D + TAKE) >> 2);
+#pragma unroll
+    for (int nb = 0; nb < NBLK; ++nb) {
+      double o[4];
+      fill4(b0 + (uint32_t)nb, o);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int idx = TAKE + 4 * nb + q;
+        if (idx < D) z[idx] = o[q];
+        else buf[idx - D] = o[q];
+      }
+    }
+  }
   // the same block schedule as NativeDraws::normals
   __device__ void normals(int k, double* z) {
     if (D == 1 || D == 2) {
@@ -52,7 +77,7 @@ struct DrawsF64 {
       if (pos == 0) fill4((uint32_t)((k * D) >> 2), buf);
       z[0] = buf[pos];
       if (D == 2) z[1] = buf[pos + 1];
-    } else {
+    } else if (D % 4 == 0 || D == 7) {
       constexpr int NB = (D + 3) / 4;
 #pragma unroll
       for (int b = 0; b < NB; ++b) {
@@ -61,6 +86,13 @@ struct DrawsF64 {
 #pragma unroll
         for (int q = 0; q < 4; ++q)
           if (4 * b + q < D) z[4 * b + q] = o[q];
+      }
+    } else {
+      switch ((k * D) & 3) {
+        case 0: dense_step<0>(k, z); break;
+        case 1: dense_step<1>(k, z); break;
+        case 2: dense_step<2>(k, z); break;
+        default: dense_step<3>(k, z); break;
       }
     }
   }

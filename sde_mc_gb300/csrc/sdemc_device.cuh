@@ -240,7 +240,42 @@ struct NativeDraws {
     o[2] = r1 * __cosf(a1); o[3] = r1 * __sinf(a1);
   }
 
+  // Step k of a dense stream (ZD not a multiple of 4): normals k ZD ..
+  // k ZD + ZD - 1 of the path's diffusion stream.  O = (k ZD) mod 4 says how
+  // many normals the previous step left in buf (4 - O, or none when O = 0);
+  // they come first, then new blocks, and the unused tail of the last new
+  // block is carried to the next step.  O is a template argument so every
+  // register index is static.
+  template <int O>
+  SDEMC_DI void dense_step(int k, float* z) {
+    constexpr int ZD = L::ZD;
+    constexpr int NC = O == 0 ? 0 : 4 - O;
+    constexpr int TAKE = NC < ZD ? NC : ZD;
+    constexpr int NBLK = (ZD - TAKE + 3) / 4;
+    float carry[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) carry[j] = buf[j];
+#pragma unroll
+    for (int j = 0; j < TAKE; ++j) z[j] = carry[j];
+    const uint32_t b0 = (uint32_t)((k * ZD + TAKE) >> 2);
+#pragma unroll
+    for (int nb = 0; nb < NBLK; ++nb) {
+      float o[4];
+      fill4(b0 + (uint32_t)nb, o);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int idx = TAKE + 4 * nb + q;
+        if (idx < ZD) z[idx] = o[q];
+        else buf[idx - ZD] = o[q];
+      }
+    }
+  }
+
   // Raw standard normals of step k (k is warp-uniform in lock-step loops).
+  // The path's diffusion stream is read densely for ZD in {1, 2, 3, 5, 6}:
+  // step k takes its normals k ZD .. k ZD + ZD - 1, four per Philox block, so
+  // no normal is discarded; ZD = 4, 8 use whole blocks anyway, and ZD = 7
+  // takes the first seven normals of two blocks per step.
   SDEMC_DI void normals(int k, float* z) {
     constexpr int ZD = L::ZD;
     if (ZD == 1 || ZD == 2) {
@@ -251,7 +286,10 @@ struct NativeDraws {
       } else {
         z[0] = buf[0]; z[1] = buf[1]; buf[0] = buf[2]; buf[1] = buf[3];
       }
-    } else {
+    } else if (ZD % 4 == 0 || ZD == 7) {
+      // whole blocks per step (for ZD = 7 one normal of every second block
+      // is left unused: the carried state would cost the served kernels more
+      // registers than the eighth of a block it saves)
 #pragma unroll
       for (int b = 0; b < L::NB; ++b) {
         float o[4];
@@ -259,6 +297,13 @@ struct NativeDraws {
 #pragma unroll
         for (int q = 0; q < 4; ++q)
           if (4 * b + q < ZD) z[4 * b + q] = o[q];
+      }
+    } else {
+      switch ((k * ZD) & 3) {
+        case 0: dense_step<0>(k, z); break;
+        case 1: dense_step<1>(k, z); break;
+        case 2: dense_step<2>(k, z); break;
+        default: dense_step<3>(k, z); break;
       }
     }
   }

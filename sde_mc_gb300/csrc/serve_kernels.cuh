@@ -190,8 +190,14 @@ struct DeltaCvSink {
   }
 };
 
+// Register budget: 80 per thread (24 resident warps per SM) for d <= 4; the
+// d >= 5 classes, which spill 76-126 bytes per thread at 80, get 128 (16
+// warps), which measured faster on the served stream than 80 for every d or
+// 128 from d = 3 on.
+template <int D> struct ServeMinBlocks { static constexpr int value = D >= 5 ? 2 : 3; };
+
 template <int D, int NOISE, int MODE, int KIND>
-__global__ void __launch_bounds__(256, 3)
+__global__ void __launch_bounds__(256, ServeMinBlocks<D>::value)
 serve_kernel(const __grid_constant__ ServeParams P) {
   __shared__ __align__(16) sdemc_inst s_inst[kServeMaxWarps];  // 16-byte aligned arrays: vector loads
   __shared__ float s_beta[kServeMaxWarps][2 * D + 1];

@@ -49,6 +49,18 @@ def test_batch_mixed_models_and_shapes():
         np.testing.assert_array_equal(plan.run().cpu().numpy(), ref)
 
 
+def test_batch_class_with_one_seed_and_with_several():
+    """A class whose instances share a seed takes the Philox round keys as
+    launch constants, a class with several seeds derives them per instance:
+    both give every instance the bits it gets alone."""
+    same = [inst_for(merton1d(40), num_paths=n, seed=5, path_offset=3 * n) for n in (64, 1000, 4097)]
+    mixed = [inst_for(merton1d(40), num_paths=n, seed=s, path_offset=0) for n, s in ((64, 5), (1000, 6), (4097, 2 ** 40 + 7))]
+    for insts in (same, mixed):
+        plan = B.BatchPlan(insts)
+        np.testing.assert_array_equal(plan.run().cpu().numpy(), alone(insts))
+        assert plan.header.n_class == 1
+
+
 def test_batch_graph_replay_with_new_offsets():
     mix = small_mix(24)
     insts = B.lower_mix(mix)
