@@ -32,18 +32,16 @@ struct NetCvSink {
   uint32_t* phase;
   bool* fail;
   float rate;
-  float xp[D], tp, range_acc, total;
+  float range_acc, total;
 
-  template <int DD> SDEMC_DI void init(const float* x) {
-#pragma unroll
-    for (int i = 0; i < D; ++i) xp[i] = x[i];
-    tp = 0.f;
+  template <int DD> SDEMC_DI void init(const float*) {
     range_acc = 0.f;
     total = 0.f;
   }
+  // xp, tp: the state and time at the start of step k
   template <int DD, int NW>
-  SDEMC_DI void step(int k, const float*, const float* x, float t, float, int, const float* dW, const float*,
-                     const float*, int) {
+  SDEMC_DI void step(int k, const float*, const float*, float, float, int, const float* dW, const float*,
+                     const float*, int, const float* xp, float tp) {
     if (k > 0 && k % kCvRange == 0) {  // k is uniform over the CTA
       total = __fadd_rn(total, range_acc);
       range_acc = 0.f;
@@ -55,9 +53,6 @@ struct NetCvSink {
       for (int i = 0; i < D; ++i) a = __fmaf_rn(o[i], dW[i], a);
       range_acc = __fadd_rn(range_acc, __fmul_rn(expf(-tp * rate), a));
     }
-#pragma unroll
-    for (int i = 0; i < D; ++i) xp[i] = x[i];
-    tp = t;
   }
   template <int DD, int NW> SDEMC_DI void finish(int, const float*, float) {}
   SDEMC_DI float value() const { return __fadd_rn(total, range_acc); }

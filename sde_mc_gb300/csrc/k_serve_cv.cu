@@ -134,9 +134,9 @@ struct CvTraceSink {
   }
   template <int DD, int NW>
   SDEMC_DI void step(int k, const float* xl, const float* x, float t, float J, int sel, const float* dW,
-                     const float* dW2, const float* zr, int jump_one) {
-    const bool live = cv.tp < T;  // the step started before T
-    cv.template step<DD, NW>(k, xl, x, t, J, sel, dW, dW2, zr, jump_one);
+                     const float* dW2, const float* zr, int jump_one, const float* xp, float tp) {
+    const bool live = tp < T;  // the step started before T
+    cv.template step<DD, NW>(k, xl, x, t, J, sel, dW, dW2, zr, jump_one, xp, tp);
     if (!live) return;
     if (k > 0 && (k & (kWeightEvery - 1)) == 0) record(k / kWeightEvery);
     if (z) {

@@ -100,7 +100,7 @@ struct TiledStoreSink {
 
   template <int Dd, int NWd>
   SDEMC_DI void step(int k, const float* xl, const float* x, float t, float J, int sel,
-                     const float* dW, const float* dW2, const float*, int jump_one) {
+                     const float* dW, const float* dW2, const float*, int jump_one, const float*, float) {
     if (k >= S) return;
     const int lane = threadIdx.x & 31, kk = k % kT;
 #pragma unroll

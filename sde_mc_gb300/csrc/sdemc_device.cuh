@@ -575,7 +575,7 @@ struct NullSink {
   static constexpr bool kWantsLeft = false;
   template <int D> SDEMC_DI void init(const float*) {}
   template <int D, int NW> SDEMC_DI void step(int, const float*, const float*, float, float, int,
-                                              const float*, const float*, const float*, int) {}
+                                              const float*, const float*, const float*, int, const float*, float) {}
   template <int D, int NW> SDEMC_DI void finish(int, const float*, float) {}
 };
 
@@ -595,7 +595,7 @@ struct StoreSink {
   }
   template <int D, int NW>
   SDEMC_DI void step(int k, const float* xl, const float* x, float t, float J, int sel,
-                     const float* dW, const float* dW2, const float* zr, int jump_one) {
+                     const float* dW, const float* dW2, const float* zr, int jump_one, const float*, float) {
     if (k >= S) return;
     const size_t c = (size_t)(k + 1) * D;
     if (paths) for (int i = 0; i < D; ++i) paths[c + i] = x[i];
@@ -660,9 +660,13 @@ SDEMC_DI int simulate(const sdemc_inst& I, Draws& dr, Sink& sk, float* x, int ma
     const float h = I.h;
     for (; k < I.num_steps; ++k) {
       dr.increments(I, k, h, dW, dW2, z);
+      float old[D];
+#pragma unroll
+      for (int i = 0; i < D; ++i) old[i] = x[i];
       euler<D, NOISE, EXACT>(I, x, h, dW, dW2);
+      const float t0 = t;
       t = __fadd_rn(t, h);
-      sk.template step<D, L::NW>(k, x, x, t, 0.f, 0, dW, dW2, z, 0);
+      sk.template step<D, L::NW>(k, x, x, t, 0.f, 0, dW, dW2, z, 0, old, t0);
     }
     sk.template finish<D, L::NW>(k, x, t);
     return k;
@@ -688,6 +692,7 @@ SDEMC_DI int simulate(const sdemc_inst& I, Draws& dr, Sink& sk, float* x, int ma
 #pragma unroll
     for (int i = 0; i < D; ++i) old[i] = x[i];
     euler<D, NOISE, EXACT>(I, x, dt, dW, dW2);
+    const float t0 = t;
     t = __fadd_rn(t, dt);
     float xl[D];
     if (Sink::kWantsLeft) {
@@ -700,7 +705,7 @@ SDEMC_DI int simulate(const sdemc_inst& I, Draws& dr, Sink& sk, float* x, int ma
       nj = dr.on_fire(I, k, nj, J, sel);
       apply_jump<D, EXACT>(I, x, I.exact_jumps ? x : old, J, sel);
     }
-    sk.template step<D, L::NW>(k, Sink::kWantsLeft ? xl : x, x, t, J, sel, dW, dW2, z, jump_one);
+    sk.template step<D, L::NW>(k, Sink::kWantsLeft ? xl : x, x, t, J, sel, dW, dW2, z, jump_one, old, t0);
     own += act ? 1 : 0;
     if (MODE & kModeNominal) {
       if (act && own == I.num_steps) {

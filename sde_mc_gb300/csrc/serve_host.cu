@@ -501,6 +501,10 @@ int Server::enqueue(TickBuf& B, const TickBuf& prev) {
     P.chunk_end = B.entries_h[j - 1].chunk_begin + B.entries_h[j - 1].nchunks;
     P.counter = B.counters_d + key;
     P.part = B.part_d;
+    P.uniform_seed = 1;
+    for (int e = k + 1; e < j; ++e)
+      if (hs[B.entries_h[e].slot].req.inst.seed != I.seed) P.uniform_seed = 0;
+    P.rk = make_round_keys(I.seed);
     const int64_t chunks = P.chunk_end - P.chunk_begin;
     cudaStream_t ks = nside > 0 ? B.side[launched % nside] : stream;
     if (E0.kind == kKindPlain)

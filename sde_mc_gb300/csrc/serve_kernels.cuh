@@ -96,7 +96,21 @@ struct ServeParams {
   int64_t chunk_begin, chunk_end;
   unsigned long long* counter;
   double* part;
+  // when every entry of the class has the same seed, the Philox round keys as
+  // launch constants (the d = 5, 6 control-variate classes use them; the
+  // others derive the keys from the seed per chunk: with constant keys the
+  // compiler holds them in registers, which spills at d = 7, 8 and d <= 4)
+  int32_t uniform_seed;
+  RoundKeys rk;
 };
+
+template <class KS> SDEMC_DI KS serve_keys(const ServeParams& P, const sdemc_inst& I);
+template <> SDEMC_DI SeedKeys serve_keys<SeedKeys>(const ServeParams&, const sdemc_inst& I) {
+  return SeedKeys{(uint32_t)I.seed, (uint32_t)(I.seed >> 32)};
+}
+template <> SDEMC_DI ConstKeys serve_keys<ConstKeys>(const ServeParams& P, const sdemc_inst&) {
+  return ConstKeys{&P.rk};
+}
 
 // The control variate's regressors, per asset i:
 //   r_i     = sum_k w_k X^i_k dW^i_k
@@ -122,22 +136,23 @@ template <int D>
 struct DeltaCvSink {
   static constexpr bool kWantsLeft = false;
   const CvWeights* cw;
-  float xp[D], r[D], a[D];
-  float tp, w, g, ag;
+  float r[D], a[D];
+  float w, g, ag;
 
-  SDEMC_DI void weights() {
+  // (w, g) at time ts and state xs
+  SDEMC_DI void weights(const float* xs, float ts) {
     if (cw->wkind == 0) { w = 1.f; g = 1.f; return; }
-    float m = xp[0];
+    float m = xs[0];
     if (cw->agg == 1) {
 #pragma unroll
-      for (int i = 1; i < D; ++i) m = __fadd_rn(m, xp[i]);
+      for (int i = 1; i < D; ++i) m = __fadd_rn(m, xs[i]);
       m = __fmul_rn(m, 1.f / (float)D);
     } else if (cw->agg == 2) {
 #pragma unroll
-      for (int i = 1; i < D; ++i) m = fmaxf(m, xp[i]);
+      for (int i = 1; i < D; ++i) m = fmaxf(m, xs[i]);
     }
     m = __fmul_rn(m, cw->scale_over_k);
-    const float tau = fmaxf(__fsub_rn(cw->T, tp), 1e-6f);
+    const float tau = fmaxf(__fsub_rn(cw->T, ts), 1e-6f);
     const float is = __fmul_rn(rsqrtf(tau), cw->inv_sig);
     if (m > 0.f) {
       const float d1 = __fmul_rn(__fmaf_rn(cw->drift, tau, __logf(m)), is);
@@ -152,15 +167,16 @@ struct DeltaCvSink {
 
   template <int DD> SDEMC_DI void init(const float* x) {
 #pragma unroll
-    for (int i = 0; i < D; ++i) { xp[i] = x[i]; r[i] = 0.f; a[i] = 0.f; }
-    tp = 0.f;
+    for (int i = 0; i < D; ++i) { r[i] = 0.f; a[i] = 0.f; }
     ag = 0.f;
-    weights();
+    weights(x, 0.f);
   }
+  // xp, tp: the state and time at the start of step k (after the previous
+  // step's jump); t: the time at its end.
   template <int DD, int NW>
-  SDEMC_DI void step(int k, const float*, const float* x, float t, float J, int sel, const float* dW, const float*,
-                     const float*, int jump_one) {
-    if (k > 0 && (k & (kWeightEvery - 1)) == 0) weights();  // k is warp-uniform
+  SDEMC_DI void step(int k, const float*, const float*, float t, float J, int sel, const float* dW, const float*,
+                     const float*, int jump_one, const float* xp, float tp) {
+    if (k > 0 && (k & (kWeightEvery - 1)) == 0) weights(xp, tp);  // k is warp-uniform
 #pragma unroll
     for (int i = 0; i < D; ++i) r[i] = __fmaf_rn(xp[i], __fmul_rn(w, dW[i]), r[i]);
     if (cw->jumps) {
@@ -176,9 +192,6 @@ struct DeltaCvSink {
         ag = __fmaf_rn(-g, __fmul_rn(__fmul_rn(J, J), cw->inv_comp_j2), ag);
       }
     }
-#pragma unroll
-    for (int i = 0; i < D; ++i) xp[i] = x[i];
-    tp = t;
   }
   template <int DD, int NW> SDEMC_DI void finish(int, const float*, float) {}
 
@@ -196,7 +209,7 @@ struct DeltaCvSink {
 // 128 from d = 3 on.
 template <int D> struct ServeMinBlocks { static constexpr int value = D >= 5 ? 2 : 3; };
 
-template <int D, int NOISE, int MODE, int KIND>
+template <int D, int NOISE, int MODE, int KIND, class KS>
 __global__ void __launch_bounds__(256, ServeMinBlocks<D>::value)
 serve_kernel(const __grid_constant__ ServeParams P) {
   __shared__ __align__(16) sdemc_inst s_inst[kServeMaxWarps];  // 16-byte aligned arrays: vector loads
@@ -250,8 +263,8 @@ serve_kernel(const __grid_constant__ ServeParams P) {
     const sdemc_inst& I = s_inst[wid];
     const int64_t p = base + (gc - lo) * kChunk + lane;
     const bool valid = p < end;
-    NativeDraws<D, NOISE, SeedKeys> dr;
-    dr.init(I, (uint64_t)p, SeedKeys{(uint32_t)I.seed, (uint32_t)(I.seed >> 32)});
+    NativeDraws<D, NOISE, KS> dr;
+    dr.init(I, (uint64_t)p, serve_keys<KS>(P, I));
     float x[D];
     if (KIND == kKindPlain) {
       NullSink sk;
@@ -307,7 +320,10 @@ serve_kernel(const __grid_constant__ ServeParams P) {
 
 template <int D, int NOISE, int MODE, int KIND>
 int launch_serve_t(const ServeParams& P, int threads, int64_t chunks, cudaStream_t s) {
-  auto kern = serve_kernel<D, NOISE, MODE, KIND>;
+  auto kern = serve_kernel<D, NOISE, MODE, KIND, SeedKeys>;
+  if constexpr ((D == 5 || D == 6) && KIND != kKindPlain) {
+    if (P.uniform_seed) kern = serve_kernel<D, NOISE, MODE, KIND, ConstKeys>;
+  }
   int per_sm = 0;
   int rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0), "occupancy query");
   if (rc) return rc;
