@@ -831,7 +831,7 @@ def bench_served(dev, steps, warmup, plain_windows, rank=0, world=1):
     import torch
     from sde_mc_gb300 import serve
     from sde_mc_gb300 import stream as S
-    srv = serve.Server(max_slots=4096, mem_budget=40 << 30, side_streams=4, policy="srpt", device=dev)
+    srv = serve.Server(max_slots=4096, mem_budget=40 << 30, side_streams=8, policy="srpt", device=dev)
     warm = shard(stream_windows(0, warmup), rank, world)
     S.run_served(warm, srv)
     timed = shard(stream_windows(warmup, steps), rank, world)
@@ -855,7 +855,7 @@ def bench_served(dev, steps, warmup, plain_windows, rank=0, world=1):
     burst = [copy.copy(r) for r in timed]
     for r in burst:
         r.t = 0.0
-    srv = serve.Server(max_slots=4096, mem_budget=40 << 30, side_streams=4, policy="srpt", device=dev)
+    srv = serve.Server(max_slots=4096, mem_budget=40 << 30, side_streams=8, policy="srpt", device=dev)
     c0 = srv.stats()
     _, csumm = S.run_served(burst, srv)
     c1 = srv.stats()
@@ -881,7 +881,7 @@ def profile_serve(seconds):
     from sde_mc_gb300 import serve
     from sde_mc_gb300 import stream as S
     reqs = S.make_stream(RATE, seconds, seed=1)
-    with serve.Server(max_slots=4096, mem_budget=40 << 30, side_streams=4, policy="srpt") as srv:
+    with serve.Server(max_slots=4096, mem_budget=40 << 30, side_streams=8, policy="srpt") as srv:
         res, summ = S.run_served(reqs, srv)
         st = srv.stats()
     torch.cuda.synchronize()
@@ -1001,7 +1001,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": busy * 1e3 / args.steps, "higher_is_better": True,
         "scaling": "strong", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "form": "served: continuous-batching server (SRPT ticks, 4 side streams, "
+        "config": {"workload": WORKLOAD, "form": "served: continuous-batching server (SRPT ticks, up to 4 in flight, 8 side streams each, "
                                               "40 GB admission budget) + delta-weighted regression control "
                                               "variate on every request",
                    "requests": n_req, "windows": args.steps, "window_s": WINDOW_S, "arrival_rate": RATE,

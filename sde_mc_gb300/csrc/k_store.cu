@@ -23,7 +23,7 @@ extern "C" int sdemc_materialise(const sdemc_inst* h_inst, int steps_cap, float*
   if (I.grid == SDEMC_GRID_UNIFORM && steps_cap < I.num_steps)
     return fail(SDEMC_EINVAL, "steps_cap %d < num_steps %d", steps_cap, I.num_steps);
   if (I.num_paths == 0) return SDEMC_OK;
-  const unsigned blocks = (unsigned)((I.num_paths + 127) / 128);
+  const unsigned blocks = (unsigned)((I.num_paths + kStoreThreads - 1) / kStoreThreads);
   cudaStream_t s = (cudaStream_t)stream;
   const int mi = max_iterations(&I);
   StoreParams P;

@@ -23,17 +23,29 @@ struct StoreParams {
 // instruction).  The padding rows after the loop (the terminal state repeated
 // to S, zero normals) go the same way.  Called in lock-step: k is the same in
 // every lane of the warp.
+// Segment length: the time the stores take follows the number of path
+// segments written (a warp's store instruction covers 128 / (4 kT D) paths),
+// so a tile holds up to 32 / D steps (128 B of one path's state per segment),
+// within 48 KB of static shared memory for the CTA's two warps.
+constexpr int kStoreThreads = 64;
+constexpr int kStoreLaneFloats = 48 * 1024 / 4 / kStoreThreads;  // 192
+
 template <int D, int NW>
 struct TiledStoreSink {
   static constexpr bool kWantsLeft = true;
-  static constexpr int kT = (16 / D) > 2 ? 16 / D : 2;  // rows per tile: >= 64 B of a path's state
   static constexpr int kRowW = 3 * D + 1;             // paths, left, jumps (D each), time
   static constexpr int kNw = D * NW;                  // normals per step
   static constexpr int kW = kRowW + kNw;
-  static constexpr int kLaneStride = kT * kW + 1;  // odd: a lane's writes and the flush reads spread over banks
+  static constexpr int kTWant = (32 / D) > 2 ? 32 / D : 2;
+  static constexpr int odd_stride(int kt) { return kt * kW + ((kt * kW) % 2 == 0 ? 1 : 2); }
+  // rows per tile; the lane stride is odd, so a lane's writes and the flush
+  // reads spread over the banks
+  static constexpr int kT = odd_stride(kTWant) <= kStoreLaneFloats ? kTWant : (kTWant / 2 > 2 ? kTWant / 2 : 2);
+  static constexpr int kLaneStride = odd_stride(kT);
+  static_assert(kLaneStride <= kStoreLaneFloats, "tile exceeds the static shared memory");
   static constexpr int kTileFloats = 32 * kLaneStride;
   float *paths, *left, *time, *jumps, *normals;
-  float* tile;       // this warp's 32 lanes x (kT x kW + 1) floats
+  float* tile;       // this warp's 32 lanes x kLaneStride floats
   int64_t p0;        // path of lane 0
   int64_t n;         // num_paths
   int S;
@@ -153,15 +165,18 @@ struct TiledStoreSink {
   }
 };
 
-template <int D, int NOISE, int MODE>
-__global__ void __launch_bounds__(128)
+// EXPORT: the raw draws and the jump stream are exported for the oracle
+// (per-lane row stores); otherwise the tiled stores only, compiled apart so the
+// export code adds no registers to the layout kernel.
+template <int D, int NOISE, int MODE, bool EXPORT>
+__global__ void __launch_bounds__(kStoreThreads)
 materialise_kernel(const __grid_constant__ StoreParams P, int S, float* paths, float* left,
                    float* time, float* jumps, float* normals, float* payoffs, int32_t* steps,
                    float* zout, int zdim, float* jt, float* jm, int32_t* jsel, int jcap,
                    int32_t* status, int max_iters) {
   using L = Layout<D, NOISE>;
   using Tiled = TiledStoreSink<D, L::NW>;
-  __shared__ float tiles[4][Tiled::kTileFloats];
+  __shared__ float tiles[kStoreThreads / 32][Tiled::kTileFloats];
   const sdemc_inst& I = P.I;
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = p < I.num_paths;
@@ -171,7 +186,7 @@ materialise_kernel(const __grid_constant__ StoreParams P, int S, float* paths, f
   float x[D];
   const int it = max_iters < S ? max_iters : S;
   int own;
-  if (!zout) {
+  if constexpr (!EXPORT) {
     Tiled sk;
     sk.paths = paths; sk.left = left; sk.time = time; sk.jumps = jumps; sk.normals = normals;
     sk.tile = tiles[threadIdx.x >> 5];
@@ -191,7 +206,7 @@ materialise_kernel(const __grid_constant__ StoreParams P, int S, float* paths, f
       sk.time = time ? time + row : nullptr;
       sk.jumps = jumps ? jumps + row * D : nullptr;
       sk.normals = normals ? normals + (size_t)p * S * D * L::NW : nullptr;
-      sk.z = zout + (size_t)p * S * zdim;
+      sk.z = zout ? zout + (size_t)p * S * zdim : nullptr;
     }
     own = simulate<D, NOISE, MODE>(I, dr, sk, x, it, ovf);
   }
@@ -201,7 +216,7 @@ materialise_kernel(const __grid_constant__ StoreParams P, int S, float* paths, f
   if (ovf) atomicOr(status, SDEMC_EOVERFLOW);
   // Export the jump stream (times, marks, picks) for the oracle: blocks 0, 1,
   // 2, ... of the path's jump stream, times accumulated as the loop does.
-  if (jcap > 0 && (jt || jm || jsel)) {
+  if (EXPORT && jcap > 0 && (jt || jm || jsel)) {
     float nj = inf_f();
     for (int j = 0; j < jcap; ++j) {
       JumpDraw d{0.f, 0.f, 0};
@@ -261,11 +276,14 @@ int launch_materialise_noise(const StoreParams& P, bool nominal, unsigned blocks
                              float* d_left, float* d_time, float* d_jumps, float* d_normals, float* d_payoffs,
                              int32_t* d_steps, float* d_z, float* d_jt, float* d_jm, int32_t* d_jsel, int jcap,
                              int32_t* d_status, int mi, cudaStream_t s) {
+  const bool exporting = d_z != nullptr || (jcap > 0 && (d_jt || d_jm || d_jsel));
 #define SDEMC_MAT_CASE(D_, N_)                                                                      \
   {                                                                                                 \
     constexpr int ZD = Layout<D_, N_>::ZD;                                                          \
-    auto kern = nominal ? materialise_kernel<D_, N_, kModeNominal> : materialise_kernel<D_, N_, 0>; \
-    kern<<<blocks, 128, 0, s>>>(P, steps_cap, d_paths, d_left, d_time, d_jumps, d_normals, d_payoffs, \
+    auto kern = nominal ? (exporting ? materialise_kernel<D_, N_, kModeNominal, true>                     \
+                               : materialise_kernel<D_, N_, kModeNominal, false>)                    \
+                        : (exporting ? materialise_kernel<D_, N_, 0, true> : materialise_kernel<D_, N_, 0, false>); \
+    kern<<<blocks, kStoreThreads, 0, s>>>(P, steps_cap, d_paths, d_left, d_time, d_jumps, d_normals, d_payoffs, \
                                 d_steps, d_z, ZD, d_jt, d_jm, d_jsel, jcap, d_status, mi);           \
   }
   SDEMC_DISPATCH_DIM(NOISE, P.I.dim, SDEMC_MAT_CASE)

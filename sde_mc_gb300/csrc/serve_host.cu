@@ -51,7 +51,7 @@ constexpr int kNumClassKeys = kNumKinds * 3 * 2 * SDEMC_MAX_DIM;
 constexpr int64_t kMaxSlicePaths = 1 << 18;
 constexpr int64_t kMinSlicePaths = 1 << 10;
 constexpr double kZ95 = 1.96;
-constexpr int kTickBufs = 3;  // ticks in flight at most
+constexpr int kTickBufs = 4;  // ticks in flight at most
 
 bool lcv_supported(const sdemc_inst& I) {
   return I.noise == SDEMC_NOISE_DIAG && !(I.flags & SDEMC_INST_PAYOFF_AT_NOMINAL_STEP);
@@ -221,7 +221,7 @@ CvWeights serve_cv_weights(const sdemc_inst& I) {
 
 struct Server {
   sdemc_server_cfg cfg{};
-  int threads = 128;
+  int threads = 256;
   int64_t part_cap = 0;  // doubles per tick buffer
   int64_t fixed_bytes = 0;
   ServeSlot* slots_d = nullptr;
@@ -261,7 +261,7 @@ struct Server {
 int Server::init(const sdemc_server_cfg& c) {
   cfg = c;
   if (cfg.max_slots < 1 || cfg.max_slots > 65536) return fail(SDEMC_EINVAL, "max_slots %d outside 1..65536", cfg.max_slots);
-  if (cfg.block_threads == 0) cfg.block_threads = 128;
+  if (cfg.block_threads == 0) cfg.block_threads = 256;
   if (cfg.block_threads < 32 || cfg.block_threads > 256 || cfg.block_threads % 32)
     return fail(SDEMC_EINVAL, "block_threads %d must be a multiple of 32 in [32, 256]", cfg.block_threads);
   threads = cfg.block_threads;
@@ -571,7 +571,7 @@ int Server::process(TickBuf& B) {
   cudaEventElapsedTime(&ms, B.t0, t_end);
   // place the tick on one device timeline: its end relative to the previous
   // processed tick's end (both stamps still recorded: the ring outlives the
-  // two ticks in flight), its start by its own duration; busy time is the
+  // ticks in flight), its start by its own duration; busy time is the
   // union of the tick intervals (ticks overlap)
   double end_ms = 0.0;
   if (B.seq > 0) {

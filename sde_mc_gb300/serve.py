@@ -111,8 +111,8 @@ class ServeResult:
 class Server:
     """Handle of a native pricing server on one CUDA device."""
 
-    def __init__(self, max_slots=4096, mem_budget=40 << 30, tick_work=0, slice_work=0, block_threads=128,
-                 side_streams=4, policy="srpt", device=None):
+    def __init__(self, max_slots=4096, mem_budget=40 << 30, tick_work=0, slice_work=0, block_threads=256,
+                 side_streams=8, policy="srpt", device=None):
         dev = N.require_cuda(device)
         self.device = dev
         cfg = ServerCfg(device=dev.index, max_slots=int(max_slots), mem_budget=int(mem_budget),

@@ -93,8 +93,9 @@ def test_memory_budget_limits_admission():
     reqs = [_req(i, rng_seed=5) for i in range(12)]
     with serve.Server(max_slots=64, mem_budget=1 << 30) as srv:
         fixed = srv.stats()["mem_in_use"]  # slot table and tick buffers of 64 slots
-    # room for the request state of only a few requests at a time
-    budget = fixed + (40 << 20)
+    # room for the chunk partials of one full slice in every tick buffer plus
+    # the request state of only a few requests at a time
+    budget = fixed + (64 << 20)
     with serve.Server(max_slots=64, mem_budget=budget, side_streams=0) as srv:
         for m in reqs:
             _submit(srv, m, 1e-2, "linear_cv")
