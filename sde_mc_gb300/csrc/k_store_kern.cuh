@@ -73,12 +73,13 @@ struct TiledStoreSink {
     if (!base) return;
     const int lane = threadIdx.x & 31;
     constexpr int SEG = CNT * W;
-    if (CNT > 0 && SEG <= 32 && (32 % (SEG > 0 ? SEG : 1)) == 0) {
+    constexpr int SEGD = SEG > 0 ? SEG : 1;  // the divisor when the branch below is live
+    if (CNT > 0 && SEG <= 32 && (32 % SEGD) == 0) {
       // a full tile whose segments tile the warp: every lane keeps one
       // (row, column) of the segment and walks the paths
-      constexpr int PPI = 32 / (SEG > 0 ? SEG : 1);  // paths per store instruction
-      const int q = lane % SEG, kk = q / W, f = q - kk * W;
-      const int jl = lane / SEG;
+      constexpr int PPI = 32 / SEGD;  // paths per store instruction
+      const int q = lane % SEGD, kk = q / W, f = q - kk * W;
+      const int jl = lane / SEGD;
       const int soff = kk * kW + f0 + f;
       float* dst = base + ((size_t)(p0 + jl) * rows + r0 + kk) * W + f;
       const size_t step = (size_t)PPI * rows * W;

@@ -129,13 +129,16 @@ SDEMC_DI void correlate(const sdemc_inst& I, const float* z, float sq, float* dW
   float zs[D];
 #pragma unroll
   for (int j = 0; j < D; ++j) zs[j] = __fmul_rn(z[j], sq);
-  if (D == 1) { dW[0] = zs[0]; return; }
+  if constexpr (D == 1) {
+    dW[0] = zs[0];
+  } else {
 #pragma unroll
-  for (int i = 0; i < D; ++i) {
-    float acc = __fmul_rn(chol_at(I, i, 0), zs[0]);
+    for (int i = 0; i < D; ++i) {
+      float acc = __fmul_rn(chol_at(I, i, 0), zs[0]);
 #pragma unroll
-    for (int j = 1; j <= i; ++j) acc = __fmaf_rn(chol_at(I, i, j), zs[j], acc);
-    dW[i] = acc;
+      for (int j = 1; j <= i; ++j) acc = __fmaf_rn(chol_at(I, i, j), zs[j], acc);
+      dW[i] = acc;
+    }
   }
 }
 
