@@ -489,13 +489,21 @@ def bench_materialise(dev, hbm_peak, peak_source="MEASURED_PEAKS.json hbm_gbs (c
     t = statistics.mean(ms) * 1e-3
     executed = float(bufs["steps"].double().sum())
     gbs = nbytes / t / 1e9
+    # DRAM bytes of an ncu-captured launch of these sources (a smaller case),
+    # scaled by paths: the layout's bytes grow in proportion to the paths
+    rec = profiled("materialise_kernel<2,diag>")
+    traffic = rec["dram_bytes"] * n / rec["paths"] if rec and rec.get("paths") else None
     return {"workload": "2D rainbow, 2^20 paths, AdaptedPathData layout at %d step rows" % S,
             "bytes_written": nbytes, "ms": t * 1e3, "path_steps_per_s": executed / t,
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
                          "frac": gbs / hbm_peak if hbm_peak else None,
                          "peak_source": peak_source,
                          "bytes": "the layout's arrays: (S + 1) rows x (3d + 1) floats + S rows x d floats "
-                                  "per path, + payoff and step count"},
+                                  "per path, + payoff and step count",
+                         "traffic": traffic,
+                         "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of one ncu-captured launch "
+                                         "(%s paths) scaled to %d paths; null when profiles/ holds no capture of "
+                                         "these kernel sources" % (rec.get("paths") if rec else "-", n)},
             "l2": "outputs (%.1f GB) far larger than L2" % (nbytes / 1e9)}
 
 

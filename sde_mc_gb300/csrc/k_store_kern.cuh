@@ -16,17 +16,22 @@ struct StoreParams {
 
 // AdaptedPathData stores through shared memory.  A path's rows are contiguous
 // in every array, so a lane writing its own row at each step touches one
-// 32-byte sector per lane and array for a few bytes; instead each lane
-// parks kT steps of (paths, left, jumps, time, normals) in its warp's tile and
-// the warp then writes lane after lane's kT-row segments with consecutive
-// lanes on consecutive addresses (full sectors, a few lines per store
-// instruction).  The padding rows after the loop (the terminal state repeated
-// to S, zero normals) go the same way.  Called in lock-step: k is the same in
-// every lane of the warp.
-// Segment length: the time the stores take follows the number of path
-// segments written (a warp's store instruction covers 128 / (4 kT D) paths),
-// so a tile holds up to 32 / D steps (128 B of one path's state per segment),
-// within 48 KB of static shared memory for the CTA's two warps.
+// 32-byte sector per lane and array for a few bytes; instead each lane parks
+// kT steps of (paths, left, jumps, time, normals) in its warp's tile and the
+// warp then writes lane after lane's kT-row segments with consecutive lanes on
+// consecutive addresses.  Measured on the 2D rainbow (2^20 paths, 271 rows):
+//   * the time follows the number of segments, so a tile holds up to 32 / D
+//     steps (128 B of one path's state per segment; 64-B segments took 1.6x
+//     as long, 32-B ones 3x), within 48 KB of static shared memory for the
+//     CTA's two warps (one-warp CTAs with 256-B segments were slower);
+//   * segments start on a row that is a multiple of kT (state row r in slot
+//     r % kT, normals row k in slot k % kT), so when a path's row is a whole
+//     number of lines every segment is whole lines and sectors: no partial
+//     sector reaches DRAM (its read-modify-write had cost 25 % of the written
+//     bytes in extra reads), 1.8x faster.
+// The padding rows after the loop (the terminal state repeated to S, zero
+// normals) go the same way.  Called in lock-step: k is the same in every lane
+// of the warp.
 constexpr int kStoreThreads = 64;
 constexpr int kStoreLaneFloats = 48 * 1024 / 4 / kStoreThreads;  // 192
 
@@ -52,17 +57,18 @@ struct TiledStoreSink {
 
   SDEMC_DI float& at(int kk, int lane, int f) const { return tile[lane * kLaneStride + kk * kW + f]; }
 
+  // Row 0 of the state arrays (x0, x0, 0, t = 0) goes to tile slot 0: state
+  // row r lives in slot r % kT and normals row k in slot k % kT, so every
+  // flush writes rows that start on a multiple of kT.
   template <int Dd> SDEMC_DI void init(const float* x) {
-    const int64_t p = p0 + (threadIdx.x & 31);
-    if (p >= n) return;
-    const size_t row = (size_t)p * (S + 1);
+    const int lane = threadIdx.x & 31;
 #pragma unroll
     for (int i = 0; i < D; ++i) {
-      if (paths) paths[row * D + i] = x[i];
-      if (left) left[row * D + i] = x[i];
-      if (jumps) jumps[row * D + i] = 0.f;
+      at(0, lane, i) = x[i];
+      at(0, lane, D + i) = x[i];
+      at(0, lane, 2 * D + i) = 0.f;
     }
-    if (time) time[row] = 0.f;
+    at(0, lane, 3 * D) = 0.f;
   }
 
   // One array's segments: every lane's rows [r0, r0 + cnt) of width W, from
@@ -100,70 +106,77 @@ struct TiledStoreSink {
     }
   }
 
+  // State rows [r0, r0 + cnt) (r0 a multiple of kT) from slots 0 .. cnt-1.
   template <int CNT>
-  SDEMC_DI void flush(int k0, int cnt) const {
+  SDEMC_DI void flush_state(int r0, int cnt) const {
     __syncwarp();
-    put<D, CNT>(paths, S + 1, 0, k0 + 1, cnt);
-    put<D, CNT>(left, S + 1, D, k0 + 1, cnt);
-    put<D, CNT>(jumps, S + 1, 2 * D, k0 + 1, cnt);
-    put<1, CNT>(time, S + 1, 3 * D, k0 + 1, cnt);
+    put<D, CNT>(paths, S + 1, 0, r0, cnt);
+    put<D, CNT>(left, S + 1, D, r0, cnt);
+    put<D, CNT>(jumps, S + 1, 2 * D, r0, cnt);
+    put<1, CNT>(time, S + 1, 3 * D, r0, cnt);
+    __syncwarp();
+  }
+  // Normals rows [k0, k0 + cnt) (k0 a multiple of kT).
+  template <int CNT>
+  SDEMC_DI void flush_normals(int k0, int cnt) const {
+    __syncwarp();
     put<kNw, CNT>(normals, S, kRowW, k0, cnt);
     __syncwarp();
   }
 
+  SDEMC_DI void put_state(int s, int lane, const float* x, const float* xl, float J, int sel, int jump_one,
+                          float t) const {
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      at(s, lane, i) = x[i];
+      at(s, lane, D + i) = xl[i];
+      at(s, lane, 2 * D + i) = (jump_one && i != sel) ? 0.f : J;
+    }
+    at(s, lane, 3 * D) = t;
+  }
+
+  // Step k writes state row k + 1 and normals row k; a slot group that is
+  // full is written out.
   template <int Dd, int NWd>
   SDEMC_DI void step(int k, const float* xl, const float* x, float t, float J, int sel,
                      const float* dW, const float* dW2, const float*, int jump_one, const float*, float) {
     if (k >= S) return;
-    const int lane = threadIdx.x & 31, kk = k % kT;
+    const int lane = threadIdx.x & 31, sn = k % kT, ss = (k + 1) % kT;
+    put_state(ss, lane, x, xl, J, sel, jump_one, t);
 #pragma unroll
     for (int i = 0; i < D; ++i) {
-      at(kk, lane, i) = x[i];
-      at(kk, lane, D + i) = xl[i];
-      at(kk, lane, 2 * D + i) = (jump_one && i != sel) ? 0.f : J;
       if (NW == 1) {
-        at(kk, lane, kRowW + i) = dW[i];
+        at(sn, lane, kRowW + i) = dW[i];
       } else {
-        at(kk, lane, kRowW + 2 * i) = dW[i];
-        at(kk, lane, kRowW + 2 * i + 1) = dW2[i];
+        at(sn, lane, kRowW + 2 * i) = dW[i];
+        at(sn, lane, kRowW + 2 * i + 1) = dW2[i];
       }
     }
-    at(kk, lane, 3 * D) = t;
-    if (kk == kT - 1) flush<kT>(k - kk, kT);
+    if (ss == kT - 1) flush_state<kT>(k + 2 - kT, kT);
+    if (sn == kT - 1) flush_normals<kT>(k + 1 - kT, kT);
   }
 
-  // Rows kend .. S-1: the rest of the last tile, then the terminal state (x,
-  // x, 0, t) repeated with zero normals, tile by tile.
+  // Steps kend .. S-1 are padding: the terminal state (x, x, 0, t) in state
+  // rows kend + 1 .. S and zero normals in rows kend .. S-1; then the open
+  // slot groups are written out.
   template <int Dd, int NWd>
   SDEMC_DI void finish(int kend, const float* x, float t) {
     const int lane = threadIdx.x & 31;
     if (kend > S) kend = S;
-    int k = kend;
-    if (k % kT != 0) {
-      // complete the open tile with padding rows, then write it
-      const int k0 = k - k % kT;
-      const int stop = min(S, k0 + kT);
-      for (; k < stop; ++k) fill_row(k % kT, lane, x, t);
-      flush<0>(k0, stop - k0);
+    for (int k = kend; k < S; ++k) {
+      const int sn = k % kT, ss = (k + 1) % kT;
+      put_state(ss, lane, x, x, 0.f, 0, 0, t);
+#pragma unroll
+      for (int i = 0; i < kNw; ++i) at(sn, lane, kRowW + i) = 0.f;
+      if (ss == kT - 1) flush_state<kT>(k + 2 - kT, kT);
+      if (sn == kT - 1) flush_normals<kT>(k + 1 - kT, kT);
     }
-    if (k < S) {
-      for (int kk = 0; kk < kT; ++kk) fill_row(kk, lane, x, t);
-      for (; k + kT <= S; k += kT) flush<kT>(k, kT);
-      if (k < S) flush<0>(k, S - k);
-    }
+    // rows 0 .. S of the state and 0 .. S-1 of the normals are in the tile or
+    // written; the last groups are partial unless they end on a multiple of kT
+    if ((S + 1) % kT != 0) flush_state<0>(S + 1 - (S + 1) % kT, (S + 1) % kT);
+    if (S % kT != 0) flush_normals<0>(S - S % kT, S % kT);
   }
 
-  SDEMC_DI void fill_row(int kk, int lane, const float* x, float t) const {
-#pragma unroll
-    for (int i = 0; i < D; ++i) {
-      at(kk, lane, i) = x[i];
-      at(kk, lane, D + i) = x[i];
-      at(kk, lane, 2 * D + i) = 0.f;
-    }
-    at(kk, lane, 3 * D) = t;
-#pragma unroll
-    for (int i = 0; i < kNw; ++i) at(kk, lane, kRowW + i) = 0.f;
-  }
 };
 
 // EXPORT: the raw draws and the jump stream are exported for the oracle
