@@ -86,14 +86,22 @@ struct TiledStoreSink {
       constexpr int PPI = 32 / SEGD;  // paths per store instruction
       const int q = lane % SEGD, kk = q / W, f = q - kk * W;
       const int jl = lane / SEGD;
-      const int soff = kk * kW + f0 + f;
+      const float* src = tile + jl * kLaneStride + kk * kW + f0 + f;  // path jl; + it * PPI paths
       float* dst = base + ((size_t)(p0 + jl) * rows + r0 + kk) * W + f;
       const size_t step = (size_t)PPI * rows * W;
+      if (n - p0 >= 32) {  // warp-uniform: every path of the warp is in range
 #pragma unroll
-      for (int it = 0; it < SEG; ++it) {
-        const int j = it * PPI + jl;
-        if (p0 + j < n) *dst = tile[j * kLaneStride + soff];
-        dst += step;
+        for (int it = 0; it < SEG; ++it) {
+          *dst = src[it * PPI * kLaneStride];
+          dst += step;
+        }
+      } else {
+        const int live = (int)(n - p0);  // paths of the warp in range (< 32)
+#pragma unroll
+        for (int it = 0; it < SEG; ++it) {
+          if (it * PPI + jl < live) *dst = src[it * PPI * kLaneStride];
+          dst += step;
+        }
       }
       return;
     }
