@@ -69,6 +69,34 @@ def test_result_is_the_same_alone_and_in_a_mix():
     assert st["ticks"] > 1 and st["busy_s"] > 0
 
 
+def test_requests_of_one_seed_and_of_several_give_the_same_bits():
+    """A d = 5 or 6 control-variate class whose requests share a seed takes the
+    Philox round keys as launch constants; with requests of other seeds in the
+    class it derives them per chunk.  A request's result is the same either
+    way."""
+    probes = [workloads.basket_instance(i, d, 48, 4096 + 33 * i, 1.0, [0.2 + 0.02 * j for j in range(d)], 1.0)
+              for i, d in ((1, 5), (2, 6))]
+    # small slices (the same in both servers: slices are a function of the
+    # request and the slice size) spread every phase over several ticks, so
+    # the probes' slices share class kernels with requests of other seeds
+    slice_work = 1 << 18
+    alone = {}
+    with serve.Server(max_slots=8, mem_budget=1 << 30, slice_work=slice_work) as srv:
+        for m in probes:
+            _submit(srv, m, 3e-3, "linear_cv")
+            (r,) = srv.wait(1)
+            alone[r.tag] = r.raise_for_status().key()
+    others = [workloads.basket_instance(10 + k, 5 + k % 2, 48, 4096, 1.05, [0.25] * (5 + k % 2), 1.5, seed=1000 + k)
+              for k in range(6)]
+    with serve.Server(max_slots=16, mem_budget=2 << 30, slice_work=slice_work) as srv:
+        for m in others + probes:
+            _submit(srv, m, 3e-3, "linear_cv")
+        res = {r.tag: r for r in srv.wait(len(probes) + len(others))}
+    for m in probes:
+        assert res[m.idx].key() == alone[m.idx], m.idx
+    assert all(res[m.idx].status == 0 for m in others)
+
+
 def test_linear_cv_is_unbiased_and_reduces_variance():
     m = workloads.basket_instance(11, 2, 128, 1 << 14, 1.0, [0.2, 0.3], 1.0)
     with serve.Server(max_slots=4, mem_budget=1 << 30) as srv:
