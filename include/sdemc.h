@@ -419,7 +419,12 @@ int sdemc_mlmc_replay_paths(const sdemc_inst* h_inst, int fine, int coarse, floa
  * sdemc_cv_backward: gradient of Var(Gamma) over the n selected paths
  * (sde_mc/varred.py:160-180) into d_grad, using d_gamma from a forward call on
  * the same selection; d_partials holds nparts x nparams floats.
- * sdemc_adam_step: one torch.optim.Adam step (no weight decay).             */
+ * sdemc_adam_step: one torch.optim.Adam step (no weight decay).
+ * sdemc_adam_bias: its bias corrections for step t >= 1, h_bc[0] = 1 - b1^t,
+ * h_bc[1] = sqrt(1 - b2^t) (host only, the arithmetic sdemc_adam_step uses).
+ * sdemc_adam_step_dev: the same step with the corrections read from device
+ * memory d_bc (2 floats), for CUDA graphs of many steps whose corrections
+ * the host refills between replays.                                       */
 int sdemc_cv_nparams(int dim);
 int sdemc_cv_forward(int dim, const float* d_params, const float* d_time,
                      const float* d_paths, const float* d_normals,
@@ -434,6 +439,10 @@ int sdemc_cv_backward(int dim, const float* d_params, const float* d_time,
 int sdemc_adam_step(float* d_params, const float* d_grad, float* d_m, float* d_v,
                     int nparam, int step, float lr, float beta1, float beta2,
                     float eps, void* stream);
+int sdemc_adam_bias(int step, float beta1, float beta2, float* h_bc);
+int sdemc_adam_step_dev(float* d_params, const float* d_grad, float* d_m,
+                        float* d_v, int nparam, const float* d_bc, float lr,
+                        float beta1, float beta2, float eps, void* stream);
 
 /* K6 on the 5th-generation tensor cores: the gradient of sdemc_cv_backward
  * (same arguments and partial layout, d_mult as in sdemc_cv_forward_tc),

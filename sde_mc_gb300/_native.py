@@ -95,6 +95,9 @@ _PROTOS = {
     "sdemc_cv_backward": (_I, [_I, _P, _P, _P, _P, _P, ctypes.c_int64, _I, ctypes.c_float, _P, _P, _I, _P, _P]),
     "sdemc_adam_step": (_I, [_P, _P, _P, _P, _I, _I, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                              ctypes.c_float, _P]),
+    "sdemc_adam_bias": (_I, [_I, ctypes.c_float, ctypes.c_float, _P]),
+    "sdemc_adam_step_dev": (_I, [_P, _P, _P, _P, _I, _P, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                 ctypes.c_float, _P]),
     "sdemc_batch_autotune": (_I, [_P, _P, _P, ctypes.c_size_t, _P, _P, _P, _I, _P, _I, _I, _P, _P, _P, _P, _P]),
     "sdemc_cv_backward_tc": (_I, [_I, _P, _P, _P, _P, _P, ctypes.c_int64, _I, ctypes.c_float, _P, _P, _I, _P, _P,
                                   _P]),

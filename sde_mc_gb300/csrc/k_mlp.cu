@@ -494,17 +494,32 @@ __global__ void grad_reduce_kernel(const float* __restrict__ partials, int npart
 
 // torch.optim.Adam (no weight decay, no amsgrad): m = b1 m + (1-b1) g,
 // v = b2 v + (1-b2) g^2, p -= lr/(1-b1^t) * m / (sqrt(v)/sqrt(1-b2^t) + eps).
-__global__ void adam_kernel(float* __restrict__ prm, const float* __restrict__ grad, float* __restrict__ m,
-                            float* __restrict__ v, int nparam, float lr, float b1, float b2, float eps,
-                            float bc1, float bc2_sqrt) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= nparam) return;
+SDEMC_DI void adam_update(int e, float* __restrict__ prm, const float* __restrict__ grad, float* __restrict__ m,
+                          float* __restrict__ v, float lr, float b1, float b2, float eps, float bc1,
+                          float bc2_sqrt) {
   const float gr = grad[e];
   const float mm = b1 * m[e] + (1.f - b1) * gr;
   const float vv = b2 * v[e] + (1.f - b2) * gr * gr;
   m[e] = mm;
   v[e] = vv;
   prm[e] -= (lr / bc1) * mm / (sqrtf(vv) / bc2_sqrt + eps);
+}
+
+__global__ void adam_kernel(float* __restrict__ prm, const float* __restrict__ grad, float* __restrict__ m,
+                            float* __restrict__ v, int nparam, float lr, float b1, float b2, float eps,
+                            float bc1, float bc2_sqrt) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < nparam) adam_update(e, prm, grad, m, v, lr, b1, b2, eps, bc1, bc2_sqrt);
+}
+
+// The same step with the bias corrections read from device memory (bc[0] =
+// 1 - b1^t, bc[1] = sqrt(1 - b2^t)), so a captured graph of many steps takes
+// each step's corrections from a table the host refills between replays.
+__global__ void adam_dev_kernel(float* __restrict__ prm, const float* __restrict__ grad, float* __restrict__ m,
+                                float* __restrict__ v, int nparam, float lr, float b1, float b2, float eps,
+                                const float* __restrict__ bc) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < nparam) adam_update(e, prm, grad, m, v, lr, b1, b2, eps, bc[0], bc[1]);
 }
 
 template <int D>
@@ -584,12 +599,27 @@ extern "C" int sdemc_cv_backward(int dim, const float* d_params, const float* d_
   return check_cuda(cudaGetLastError(), "grad_reduce_kernel launch");
 }
 
+extern "C" int sdemc_adam_bias(int step, float beta1, float beta2, float* h_bc) {
+  if (step < 1 || !h_bc) return fail(SDEMC_EINVAL, "bad adam_bias args");
+  h_bc[0] = 1.f - powf(beta1, (float)step);
+  h_bc[1] = sqrtf(1.f - powf(beta2, (float)step));
+  return SDEMC_OK;
+}
+
 extern "C" int sdemc_adam_step(float* d_params, const float* d_grad, float* d_m, float* d_v, int nparam, int step,
                                float lr, float beta1, float beta2, float eps, void* stream) {
   if (nparam < 1 || step < 1 || !d_params || !d_grad || !d_m || !d_v) return fail(SDEMC_EINVAL, "bad adam args");
-  const float bc1 = 1.f - powf(beta1, (float)step);
-  const float bc2 = sqrtf(1.f - powf(beta2, (float)step));
+  float bc[2];
+  sdemc_adam_bias(step, beta1, beta2, bc);
   adam_kernel<<<(nparam + 255) / 256, 256, 0, (cudaStream_t)stream>>>(d_params, d_grad, d_m, d_v, nparam, lr, beta1,
-                                                                      beta2, eps, bc1, bc2);
+                                                                      beta2, eps, bc[0], bc[1]);
   return check_cuda(cudaGetLastError(), "adam_kernel launch");
+}
+
+extern "C" int sdemc_adam_step_dev(float* d_params, const float* d_grad, float* d_m, float* d_v, int nparam,
+                                   const float* d_bc, float lr, float beta1, float beta2, float eps, void* stream) {
+  if (nparam < 1 || !d_params || !d_grad || !d_m || !d_v || !d_bc) return fail(SDEMC_EINVAL, "bad adam args");
+  adam_dev_kernel<<<(nparam + 255) / 256, 256, 0, (cudaStream_t)stream>>>(d_params, d_grad, d_m, d_v, nparam, lr,
+                                                                          beta1, beta2, eps, d_bc);
+  return check_cuda(cudaGetLastError(), "adam_dev_kernel launch");
 }

@@ -466,9 +466,9 @@ __global__ void grad_reduce_tc_kernel(const float* __restrict__ partials, int np
 
 constexpr size_t kSmemBytes = sizeof(BwdSmem) + 1024;
 
-// CTAs the backward launches for n paths of S steps (at most nparts).
+// Kernel attributes and resident CTAs per SM on device dev.
 template <int D>
-int grid_for(int64_t n, int S, int nparts, int* grid) {
+int per_sm_for(int dev, int* out) {
   auto kern = cv_backward_tc_kernel<D>;
   int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes),
                       "smem attribute");
@@ -477,9 +477,8 @@ int grid_for(int64_t n, int S, int nparts, int* grid) {
                                             (int)cudaSharedmemCarveoutMaxShared), "carveout attribute")))
     return rc;
   cudaFuncAttributes fa;
-  int dev = 0, smem_sm = 0;
+  int smem_sm = 0;
   if ((rc = check_cuda(cudaFuncGetAttributes(&fa, kern), "function attributes"))) return rc;
-  if ((rc = check_cuda(cudaGetDevice(&dev), "cudaGetDevice"))) return rc;
   if ((rc = check_cuda(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev),
                        "smem per SM")))
     return rc;
@@ -491,6 +490,24 @@ int grid_for(int64_t n, int S, int nparts, int* grid) {
   if (per_sm > by_smem) per_sm = by_smem;
   if (per_sm > (int)(512 / kCols)) per_sm = (int)(512 / kCols);
   if (per_sm < 1) per_sm = 1;
+  *out = per_sm;
+  return SDEMC_OK;
+}
+
+// CTAs the backward launches for n paths of S steps (at most nparts).  The
+// kernel attributes and the resident CTAs per SM are set up once per device,
+// so a call inside a CUDA graph capture only launches.
+template <int D>
+int grid_for(int64_t n, int S, int nparts, int* grid) {
+  static int per_sm_of[64] = {};  // per device ordinal; 0 = not set up yet
+  int dev = 0;
+  int rc = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+  if (rc) return rc;
+  int per_sm = dev < 64 ? per_sm_of[dev] : 0;
+  if (per_sm < 1) {
+    if ((rc = per_sm_for<D>(dev, &per_sm))) return rc;
+    if (dev < 64) per_sm_of[dev] = per_sm;
+  }
   const int64_t units = ((n + kRows - 1) / kRows) * ((S + kRangeLen - 1) / kRangeLen);
   int64_t ctas = (int64_t)num_sms() * per_sm;
   if (ctas > units) ctas = units;

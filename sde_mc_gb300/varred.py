@@ -201,6 +201,14 @@ class GpuCv:
                                       float(eps), N.stream_handle(self.device))
         N.check(rc, "sdemc_adam_step")
 
+    def adam_dev(self, bc, lr=1e-3, betas=(0.9, 0.999), eps=1e-8):
+        """The Adam step with its bias corrections read from device memory
+        (``bc``: 2 floats); the caller advances ``step_count``."""
+        rc = N.load().sdemc_adam_step_dev(N.ptr(self.params), N.ptr(self.grad), N.ptr(self.m), N.ptr(self.v),
+                                          self.nparam, N.ptr(bc), float(lr), float(betas[0]), float(betas[1]),
+                                          float(eps), N.stream_handle(self.device))
+        N.check(rc, "sdemc_adam_step_dev")
+
     def write_back(self, opt=None):
         """Copy the trained weights (and Adam state) into the torch objects."""
         self.f.load_flat_params(self.params)
@@ -239,36 +247,78 @@ def adam_hparams(opt):
 BACKWARD_TC = True
 
 
+# Epochs after the first replay one CUDA graph of the epoch's minibatch steps
+# (the same kernels with the same arguments, so the same bits; False: every
+# step launched from the host).
+TRAIN_GRAPH = True
+
+
 def train_gpu(cvs, datas, rate, epochs, batch_size, lr, betas, eps, print_losses=False, early_stopping=None,
               generator=None):
     """Minibatch training of the networks ``cvs`` (one data set each, same
-    paths) on Var(Gamma); returns the per-epoch mean losses."""
+    paths) on Var(Gamma); returns the per-epoch mean losses.  The first epoch
+    runs step by step; with ``TRAIN_GRAPH`` the later ones replay a graph of a
+    whole epoch captured once, the permutation and Adam's bias corrections
+    refilled in place before each replay."""
+    import ctypes
     n = datas[0].n
     nb = n // batch_size
     if nb < 1:
         raise ValueError("batch size %d larger than the %d training paths" % (batch_size, n))
     dev = cvs[0].device
+    lib = N.load()
+    perm = torch.empty(n, dtype=torch.int64, device=dev)
+    losses = torch.zeros(nb, dtype=torch.float64, device=dev)
+    gamma = torch.empty(batch_size, dtype=torch.float32, device=dev)
+    use_graph = TRAIN_GRAPH and BACKWARD_TC and epochs > 1
+    if use_graph:
+        bc_dev = [torch.empty((nb, 2), dtype=torch.float32, device=dev) for _ in cvs]
+        bc_host = [torch.empty((nb, 2), dtype=torch.float32, pin_memory=True) for _ in cvs]
+    graph = None
+
+    def minibatch(b, adam):
+        idx = perm[b * batch_size:(b + 1) * batch_size]
+        cvs[0].forward(datas[0], rate, idx, gamma)
+        for cv, data in zip(cvs[1:], datas[1:]):
+            gamma.add_(cv.forward(data, rate, idx))
+        losses[b] = gamma.double().var()
+        for cv, data in zip(cvs, datas):
+            if BACKWARD_TC:
+                cv.backward_tc(data, rate, gamma, idx)
+            else:
+                cv.backward(data, rate, gamma, idx)
+        for j, cv in enumerate(cvs):
+            adam(j, cv, b)
+
+    def eager_adam(j, cv, b):
+        cv.adam(lr, betas, eps)
+
+    def graph_adam(j, cv, b):
+        cv.adam_dev(bc_dev[j][b], lr, betas, eps)
+
     loss_arr = []
     cost = 0.0
     for epoch in range(epochs):
         t0 = time.time()
-        perm = torch.randperm(n, device=dev, generator=generator)
-        losses = torch.zeros(nb, dtype=torch.float64, device=dev)
-        gamma = torch.empty(batch_size, dtype=torch.float32, device=dev)
-        for b in range(nb):
-            idx = perm[b * batch_size:(b + 1) * batch_size]
-            cvs[0].forward(datas[0], rate, idx, gamma)
-            for cv, data in zip(cvs[1:], datas[1:]):
-                gamma += cv.forward(data, rate, idx)
-            losses[b] = gamma.double().var()
-            for cv, data in zip(cvs, datas):
-                if BACKWARD_TC:
-                    cv.backward_tc(data, rate, gamma, idx)
-                else:
-                    cv.backward(data, rate, gamma, idx)
-            for cv in cvs:
-                cv.adam(lr, betas, eps)
-        loss_arr.append(float(losses.mean()))
+        perm.copy_(torch.randperm(n, device=dev, generator=generator))
+        if use_graph and epoch > 0:
+            if graph is None:
+                graph = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(graph):  # records the launches; nothing runs here
+                    for b in range(nb):
+                        minibatch(b, graph_adam)
+            for j, cv in enumerate(cvs):
+                base = bc_host[j].data_ptr()
+                for b in range(nb):
+                    N.check(lib.sdemc_adam_bias(cv.step_count + b + 1, float(betas[0]), float(betas[1]),
+                                                ctypes.c_void_p(base + 8 * b)), "sdemc_adam_bias")
+                bc_dev[j].copy_(bc_host[j], non_blocking=True)
+                cv.step_count += nb
+            graph.replay()
+        else:
+            for b in range(nb):
+                minibatch(b, eager_adam)
+        loss_arr.append(float(losses.mean()))  # waits for the epoch (and its table copies)
         if BACKWARD_TC:
             for cv in cvs:
                 N.status_error(int(cv._bwd_status.item()), "control-variate gradient (tensor cores)")

@@ -47,6 +47,20 @@ def test_library_exports_nothing_undeclared():
     assert public == set(declared_symbols()), sorted(public ^ set(declared_symbols()))
 
 
+def test_adam_bias_corrections():
+    """The host-side bias corrections that a graph of Adam steps reads from
+    device memory: 1 - b1^t and sqrt(1 - b2^t) in float32; t < 1 refused."""
+    import ctypes
+    lib = N.load()
+    buf = (ctypes.c_float * 2)()
+    b1, b2 = float(np.float32(0.9)), float(np.float32(0.999))  # the float32 betas the call receives
+    for t in (1, 7, 640):
+        assert lib.sdemc_adam_bias(t, 0.9, 0.999, buf) == N.OK
+        assert buf[0] == pytest.approx(1 - b1 ** t, rel=2e-6)
+        assert buf[1] == pytest.approx(math.sqrt(1 - b2 ** t), rel=2e-5)
+    assert lib.sdemc_adam_bias(0, 0.9, 0.999, buf) == N.EINVAL
+
+
 def test_descriptor_layout_matches_header():
     lib = N.load()
     assert lib.sdemc_abi_version() == 1

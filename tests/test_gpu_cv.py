@@ -149,6 +149,32 @@ def test_training_reduces_variance_without_bias():
     assert abs(st_cv.sample_mean - st_plain.sample_mean) < 3 * math.hypot(st_cv.sample_std, st_plain.sample_std)
 
 
+@pytest.mark.parametrize("jumps", [False, True])
+def test_graph_epochs_equal_step_by_step_training(monkeypatch, jumps):
+    """Epochs replayed from a captured CUDA graph (Adam's bias corrections
+    read from a device table) give the bits of the step-by-step epochs:
+    losses, weights and Adam moments, for f alone and for f and g."""
+    from tests.cases import merton2d_corr
+    solver, payoff, disc = merton2d_corr(32, seed=13) if jumps else indep2d(32, seed=11)
+    dl = sm.simulate_adapted_data(1 << 14, solver, payoff, disc, bs=1024)
+    runs = []
+    for graph in (False, True):
+        monkeypatch.setattr(V, "TRAIN_GRAPH", graph)
+        f = _net(2, seed=5)
+        g = _net(2, seed=7) if jumps else sm.ZeroFunction(2)
+        params = list(f.parameters()) + (list(g.parameters()) if jumps else [])
+        opt = torch.optim.Adam(params, lr=1e-3)
+        torch.manual_seed(123)
+        losses = sm.train_adapted_control_variates([f, g], opt, dl, solver, disc, epochs=3, print_losses=False)
+        nets = [f] + ([g] if jumps else [])
+        runs.append((losses, [torch.cat([n._sdemc_gpu.params, n._sdemc_gpu.m, n._sdemc_gpu.v]).cpu() for n in nets],
+                     [n._sdemc_gpu.step_count for n in nets]))
+    assert runs[0][0] == runs[1][0]
+    assert runs[0][2] == runs[1][2] == [3 * (1 << 14) // 1024] * len(runs[0][2])
+    for a, b in zip(runs[0][1], runs[1][1]):
+        assert torch.equal(a, b)
+
+
 def test_unsupported_models_raise():
     solver, payoff, disc = indep2d(8)
     dl = sm.simulate_adapted_data(64, solver, payoff, disc, bs=64, inference=True)
