@@ -247,19 +247,22 @@ def adam_hparams(opt):
 BACKWARD_TC = True
 
 
-# Epochs after the first replay one CUDA graph of the epoch's minibatch steps
-# (the same kernels with the same arguments, so the same bits; False: every
-# step launched from the host).
-TRAIN_GRAPH = True
+# True: epochs after the first replay one CUDA graph of the epoch's minibatch
+# steps (the same kernels with the same arguments, so the same bits).  Off by
+# default: measured on one GB300, the 2^18-path, 10-epoch training took
+# 0.313 s with the graph and 0.312 s launched step by step (the loop is bound
+# by the gradient kernel, not by the host), and per-request training of 4
+# epochs was 3.5 % slower with the capture.
+TRAIN_GRAPH = False
 
 
 def train_gpu(cvs, datas, rate, epochs, batch_size, lr, betas, eps, print_losses=False, early_stopping=None,
               generator=None):
     """Minibatch training of the networks ``cvs`` (one data set each, same
-    paths) on Var(Gamma); returns the per-epoch mean losses.  The first epoch
-    runs step by step; with ``TRAIN_GRAPH`` the later ones replay a graph of a
-    whole epoch captured once, the permutation and Adam's bias corrections
-    refilled in place before each replay."""
+    paths) on Var(Gamma); returns the per-epoch mean losses.  With
+    ``TRAIN_GRAPH`` the epochs after the first replay a graph of a whole epoch
+    captured once, the permutation and Adam's bias corrections refilled in
+    place before each replay; otherwise every step is launched from the host."""
     import ctypes
     n = datas[0].n
     nb = n // batch_size
