@@ -521,7 +521,7 @@ typedef struct {
   int32_t max_slots;        /* requests resident at once (1..65536)             */
   int64_t mem_budget;       /* device bytes for slots and tick partials        */
   int64_t tick_work;        /* path-step x dim units per tick (0: 2^33)         */
-  int64_t slice_work;       /* path-step x dim units per slot slice (0: 2^28)   */
+  int64_t slice_work;       /* path-step x dim units per slot slice (0: 2^27)   */
   int32_t block_threads;    /* class-kernel CTA size, multiple of 32 (0: 256)   */
   int32_t side_streams;     /* class kernels spread over this many streams      */
   int32_t policy;           /* SDEMC_SERVE_FIFO or SDEMC_SERVE_SRPT             */

@@ -266,7 +266,7 @@ int Server::init(const sdemc_server_cfg& c) {
     return fail(SDEMC_EINVAL, "block_threads %d must be a multiple of 32 in [32, 256]", cfg.block_threads);
   threads = cfg.block_threads;
   if (cfg.tick_work <= 0) cfg.tick_work = (int64_t)1 << 33;
-  if (cfg.slice_work <= 0) cfg.slice_work = (int64_t)1 << 28;
+  if (cfg.slice_work <= 0) cfg.slice_work = (int64_t)1 << 27;  // 2,000 req/s basket stream: p50/p99 2.95/22.5 ms (2^28: 3.3/24.5, 2^26: 2.45/24.3)
   if (cfg.side_streams < 0 || cfg.side_streams > 16) return fail(SDEMC_EINVAL, "side_streams %d outside 0..16", cfg.side_streams);
   if (cfg.policy != SDEMC_SERVE_FIFO && cfg.policy != SDEMC_SERVE_SRPT) return fail(SDEMC_EINVAL, "unknown policy %d", cfg.policy);
   int rc = check_cuda(cudaSetDevice(cfg.device), "cudaSetDevice");
