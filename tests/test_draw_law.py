@@ -61,6 +61,27 @@ def test_different_seeds_streams_and_paths_give_different_draws(oracle_mod):
     np.testing.assert_array_equal(O.native_normals(a, 9, 16, 1), O.native_normals(c, 2, 16, 1))
 
 
+def test_steps_read_the_normal_stream_densely_or_by_whole_blocks(oracle_mod):
+    """A path's diffusion normals come four per Philox block, the blocks the
+    same for every dimension (the counter is block, path, stream; the key the
+    seed).  Steps of 1, 2, 3, 5 or 6 normals read the stream densely (step k
+    takes normals k ZD .. k ZD + ZD - 1); steps of 4 or 8 take whole blocks;
+    a step of 7 takes the first seven normals of its two blocks.  The
+    stream itself is the whole-block sequence at d = 4."""
+    O = oracle_mod
+    S = 24
+    stream = {p: O.native_normals(inst_for(basket(4, 16), seed=11), p, 2 * S, 4).ravel() for p in (0, 5)}
+    for d in range(1, 9):
+        inst = inst_for(basket(d, 16), seed=11)
+        for p in (0, 5):
+            z = O.native_normals(inst, p, S, d)
+            if d == 7:
+                want = stream[p][:8 * S].reshape(S, 8)[:, :7]
+            else:
+                want = stream[p][:d * S].reshape(S, d)
+            np.testing.assert_array_equal(z, want, err_msg="d=%d path %d" % (d, p))
+
+
 def _jumps(O, inst, paths, n):
     out = [O.native_jumps(inst, p, n) for p in range(paths)]
     jt = np.stack([o[0] for o in out]).astype(np.float64)
