@@ -109,7 +109,16 @@ class ServeResult:
 
 
 class Server:
-    """Handle of a native pricing server on one CUDA device."""
+    """Handle of a native pricing server on one CUDA device.
+
+    ``max_slots`` requests are resident at once and ``mem_budget`` bytes hold
+    the slot table and the tick buffers' chunk partials (admission waits for
+    both).  ``tick_work`` caps a tick's work and ``slice_work`` the work one
+    request contributes to a tick, both in path-step x dimension units (0:
+    the library's defaults, 2^33 — in effect no cap — and 2^27).  Class kernels run in
+    ``block_threads``-thread CTAs spread over ``side_streams`` streams per
+    tick; up to four ticks are in flight.  ``policy``: "srpt" (shortest
+    remaining work first) or "fifo"."""
 
     def __init__(self, max_slots=4096, mem_budget=40 << 30, tick_work=0, slice_work=0, block_threads=256,
                  side_streams=8, policy="srpt", device=None):
